@@ -1,0 +1,355 @@
+"""Benchmark: paths/s of the plain fused FP32 kernel on the drop-in workload.
+
+Workload (the configuration the headline metric is quoted on):
+  one_factor_50  N = 50 assets, one-factor covariance, 1-day horizon,
+                 M = 1e8 paths per step, Dirichlet(1) weights, portfolio
+                 threshold -3%, crash semantics x = 0.03, k = 5, seed 67,
+                 Philox normals, FP32 returns, FP64 Cholesky (done once,
+                 resident).  Synthetic inputs (numpy PCG64), no data set.
+
+A step is one pass of the fused kernel over the M paths of the batch (the
+breach and crash counts of every path, exact 64-bit integers).
+
+`value`   paths/s with the factor resident in HBM, device time of the K timed
+          kernels (CUDA events on the launching stream).  The kernel's inputs
+          are a few KB, so L2 is flushed (a 256 MB write) before every timed
+          step, outside the event pair.
+`e2e`     paths/s through the reference-facing plugin call
+          (get_cuda_model().run_model, host buffers): every step uploads mu and
+          Sigma, factors on the GPU, runs the kernel and reads the counts back.
+`roofline` the fused kernel against the measured FP32 FMA peak (rg_probe_peaks),
+          plus the composite issue bound that also charges normal generation
+          at the measured normal-generation peak.
+`cpu_baseline` the oracle's restatement of the reference's C serial model on the
+          host (1 core), bounded sample.
+
+--impl reference times the reference's CPU implementation of this path (its
+serial and OpenMP models; compiled from the reference's sources where the
+reference tree exists, else the oracle's restatement of them) on all host
+cores, on a bounded sample of the same workload.
+"""
+import argparse
+import contextlib
+import io
+import json
+import math
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, os.path.join(ROOT, "gpu-montecarlo-risk_gb300"))
+
+WORKLOAD = "one_factor_50"
+METRIC = "paths_per_second"
+UNIT = "paths/s"
+
+# DRAM bytes per launch of the fused kernel measured by ncu on the full
+# workload (profiles/mc_plain_one_factor_50.md); None until captured.
+NCU_TRAFFIC_BYTES = None
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="riskgpu", choices=["riskgpu", "reference"])
+    ap.add_argument("--paths", type=int, default=100_000_000)
+    ap.add_argument("--cpu-seconds", type=float, default=12.0,
+                    help="approximate CPU time of the bounded CPU samples")
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    return ap.parse_args()
+
+
+def dist_env():
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return rank, world, local
+
+
+def config(args, world):
+    return {"workload": WORKLOAD, "n_assets": 50, "horizon_days": 1, "paths_per_step": args.paths,
+            "factor": "one-factor", "weights": "Dirichlet(1)", "port_threshold": -0.03,
+            "x": 0.03, "k": 5, "rng": "philox4x32-10", "precision": "fp32",
+            "cholesky": "fp64 on GPU, resident", "l2": "flushed (256 MB write) before each timed step",
+            "parallelism": f"path-range shards x{world}" if world > 1 else "1 GPU"}
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons during the timed region."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index):
+        self.index = index
+        self.proc = None
+        self.path = None
+
+    def start(self):
+        try:
+            fd, self.path = tempfile.mkstemp(suffix=".csv")
+            os.close(fd)
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", f"--id={self.index}", f"--query-gpu={self.FIELDS}",
+                 "--format=csv,noheader,nounits", "-lms", "200"],
+                stdout=open(self.path, "w"), stderr=subprocess.DEVNULL)
+        except (OSError, FileNotFoundError):
+            self.proc = None
+
+    def stop(self):
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        time.sleep(0.25)
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        sm, smax, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in open(self.path):
+            parts = [p.strip() for p in line.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sm.append(float(parts[1]))
+                smax.append(float(parts[2]))
+            except ValueError:
+                continue
+            for n, v in zip(names, parts[5:9]):
+                if v.lower() == "active":
+                    reasons.add(n)
+        os.unlink(self.path)
+        return {"sm_mhz": statistics.median(sm) if sm else None,
+                "sm_max_mhz": max(smax) if smax else None, "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+@contextlib.contextmanager
+def quiet_stdout():
+    """Silence stdout at the file-descriptor level: the reference's models
+    print with C stdio, which Python's redirect does not catch."""
+    import ctypes
+    libc = ctypes.CDLL(None)
+    sys.stdout.flush()
+    libc.fflush(None)
+    saved = os.dup(1)
+    devnull = os.open(os.devnull, os.O_WRONLY)
+    os.dup2(devnull, 1)
+    try:
+        yield
+    finally:
+        libc.fflush(None)
+        os.dup2(saved, 1)
+        os.close(saved)
+        os.close(devnull)
+
+
+def cpu_sample_paths(rate_guess, seconds):
+    return max(2000, int(rate_guess * seconds))
+
+
+def run_cpu_reference(p, seconds, threads):
+    """The reference's CPU models on a bounded sample: (paths/s, details)."""
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import mc_oracle
+    mc_oracle.build()
+    use_ref = mc_oracle.ref_available()
+    kind = "reference" if use_ref else "port"
+    out = {}
+    for model, nthreads in (("serial", 1), ("openmp", threads)):
+        # calibrate on a small sample, then run ~seconds of work
+        M0 = 2000
+        t0 = time.perf_counter()
+        _cpu_run(mc_oracle, use_ref, model, p, M0, nthreads)
+        rate0 = M0 / max(time.perf_counter() - t0, 1e-6)
+        M = min(cpu_sample_paths(rate0, seconds / 2), 2_000_000_000)
+        t0 = time.perf_counter()
+        res = _cpu_run(mc_oracle, use_ref, model, p, M, nthreads)
+        dt = time.perf_counter() - t0
+        out[model] = {"paths_per_s": M / dt, "paths": M, "seconds": dt, "threads": nthreads,
+                      "count": res["count"]}
+    return kind, out
+
+
+def _cpu_run(mc_oracle, use_ref, model, p, M, nthreads):
+    os.environ["OMP_NUM_THREADS"] = str(nthreads)
+    with quiet_stdout():
+        if use_ref:
+            return mc_oracle.ref_run(model, p.mu, p.sigma, M, p.k, p.x, p.seed, keep_upper=True,
+                                     nthreads=nthreads)
+        if model == "serial":
+            return mc_oracle.serial_estimate(p.mu, p.sigma, M, p.k, p.x, p.seed, keep_upper=True)
+        return mc_oracle.omp_estimate(p.mu, p.sigma, M, p.k, p.x, p.seed, keep_upper=True,
+                                      nthreads=nthreads)
+
+
+def reference_arm(args):
+    rank, world, _ = dist_env()
+    if rank != 0:
+        return
+    from riskgpu import synth
+    p = synth.one_factor_50(n_paths=args.paths)
+    threads = os.cpu_count() or 1
+    times, kinds, details = [], None, None
+    # warm-up + K timed steps, each a bounded sample of the workload
+    per_step = max(1.0, args.cpu_seconds / max(1, args.steps))
+    for i in range(args.warmup + args.steps):
+        kind, det = run_cpu_reference(p, per_step if i >= args.warmup else 0.5, threads)
+        if i >= args.warmup:
+            best = max(det.values(), key=lambda d: d["paths_per_s"])
+            times.append(best["paths_per_s"])
+            kinds, details = kind, det
+    value = statistics.median(times)
+    best_model = max(details, key=lambda m: details[m]["paths_per_s"])
+    sample = (f"{details[best_model]['paths']} paths of the {WORKLOAD} workload per step with the "
+              f"reference's {best_model} model ({details[best_model]['threads']} threads); "
+              f"serial {details['serial']['paths_per_s']:.4g} paths/s, openmp "
+              f"{details['openmp']['paths_per_s']:.4g} paths/s")
+    line = {"impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * args.paths / value,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+            "data": "synthetic", "config": config(args, world),
+            "cpu_baseline": {"value": value, "unit": UNIT, "cores": details[best_model]["threads"],
+                             "kind": kinds, "sample": sample},
+            "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
+def engine_arm(args):
+    import torch
+    import riskgpu
+    from riskgpu import synth
+
+    rank, world, local = dist_env()
+    torch.cuda.set_device(local)
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl")
+
+    def barrier():
+        if dist is not None:
+            dist.barrier()
+
+    p = synth.one_factor_50(n_paths=args.paths)
+    stream = torch.cuda.Stream()
+    sp = stream.cuda_stream
+    port = riskgpu.Portfolio(p.mu, p.sigma, p.weights)
+    counts = torch.zeros(2, dtype=torch.int64, device="cuda")
+    flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda")
+    # shard: rank r owns paths [r*M, (r+1)*M)
+    q = riskgpu.make_query(args.paths, p.seed, x=p.x, k=p.k, horizon=1,
+                           port_threshold=p.port_threshold, path_offset=rank * args.paths,
+                           precision=riskgpu.PREC_FP32)
+
+    with torch.cuda.stream(stream):
+        for _ in range(args.warmup):
+            port.launch_counts(q, counts.data_ptr(), sp)
+        torch.cuda.synchronize()
+        ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True))
+              for _ in range(args.steps)]
+        clocks = ClockSampler(torch.cuda.current_device())
+        clocks.start()
+        barrier()
+        torch.cuda.synchronize()
+        wall0 = time.perf_counter()
+        results = []
+        for i in range(args.steps):
+            flush.fill_(float(i))
+            ev[i][0].record(stream)
+            port.launch_counts(q, counts.data_ptr(), sp)
+            ev[i][1].record(stream)
+        torch.cuda.synchronize()
+        barrier()
+        wall = time.perf_counter() - wall0
+        clk = clocks.stop()
+    step_ms = [a.elapsed_time(b) for a, b in ev]
+    total_ms = sum(step_ms)
+    crash, breach = [int(v) for v in counts.cpu().tolist()]
+    if dist is not None:
+        t = torch.tensor([total_ms], device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        total_ms = float(t.item())
+    value = world * args.paths * args.steps / (total_ms * 1e-3)
+    ms_per_step = total_ms / args.steps
+
+    # ---- e2e through the reference-facing plugin call (host buffers)
+    call = riskgpu.PluginCall(p.mu, p.sigma)
+    e2e_steps = max(3, min(args.steps, 5))
+    os.environ.pop("RG_MATERIALIZE_S", None)
+    os.environ.pop("RG_RNG", None)
+    with quiet_stdout():
+        call.run(args.paths, p.k, p.x, p.seed)  # warm-up
+        barrier()
+        t0 = time.perf_counter()
+        for _ in range(e2e_steps):
+            r = call.run(args.paths, p.k, p.x, p.seed)
+            if r["status"] != 0:
+                raise RuntimeError("plugin call failed")
+        barrier()
+        e2e_s = (time.perf_counter() - t0) / e2e_steps
+    h2d = 8 * p.n + 8 * p.n * p.n
+    d2h = 16 + 4 + 16  # counts, Cholesky info, portfolio moments
+
+    # ---- roofline of the fused kernel
+    peaks = riskgpu.probe_peaks(sp)
+    torch.cuda.synchronize()
+    n = p.n
+    flops_per_path = n * (n + 1) + 2 * n          # triangular contraction + w.R
+    normals_per_path = 4 * ((n + 3) // 4)          # one Philox block per 4 assets
+    achieved = flops_per_path * args.paths / (ms_per_step * 1e-3) / 1e12
+    t_ideal = (flops_per_path / (peaks["fp32_tflops"] * 1e12)
+               + normals_per_path / peaks["normals_per_s"]) * args.paths
+    roofline = {"bound": "alu", "kernel": "mc_plain_small_kernel<64,philox>",
+                "achieved": achieved, "peak": peaks["fp32_tflops"], "unit": "TFLOP/s",
+                "frac": achieved / peaks["fp32_tflops"],
+                "peak_source": "measured live: FP32 FMA micro-kernel (rg_probe_peaks)",
+                "composite_frac": t_ideal / (ms_per_step * 1e-3),
+                "normals_per_s": normals_per_path * args.paths / (ms_per_step * 1e-3),
+                "normals_peak": peaks["normals_per_s"],
+                "algorithmic_flops_per_path": flops_per_path,
+                "traffic": NCU_TRAFFIC_BYTES}
+
+    line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": ms_per_step, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+            "config": config(args, world),
+            "e2e": {"value": world * args.paths / e2e_s, "unit": UNIT, "h2d_bytes_per_step": h2d,
+                    "d2h_bytes_per_step": d2h, "ms_per_step": 1e3 * e2e_s,
+                    "path": "get_cuda_model().run_model (host mu/Sigma)"},
+            "gpu_launches": args.steps, "clocks": clk, "roofline": roofline,
+            "wall_s_timed_region": wall, "counts_last_step": {"crash": crash, "breach": breach},
+            "step_ms": [round(v, 4) for v in step_ms]}
+    if rank == 0 and world == 1 and not args.no_cpu_baseline:
+        kind, det = run_cpu_reference(p, args.cpu_seconds, os.cpu_count() or 1)
+        s = det["serial"]
+        line["cpu_baseline"] = {"value": s["paths_per_s"], "unit": UNIT, "cores": 1, "kind": kind,
+                                "sample": f"{s['paths']} paths of {WORKLOAD}, reference serial model "
+                                          f"(MT19937 + polar normals + FP64 dgemv), 1 thread",
+                                "openmp_all_cores": {"value": det["openmp"]["paths_per_s"],
+                                                     "cores": det["openmp"]["threads"]}}
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+    port.close()
+    if dist is not None:
+        dist.destroy_process_group()
+
+
+def main():
+    args = parse()
+    if args.impl == "reference":
+        reference_arm(args)
+    else:
+        engine_arm(args)
+
+
+if __name__ == "__main__":
+    main()

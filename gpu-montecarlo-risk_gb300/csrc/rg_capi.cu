@@ -1,0 +1,515 @@
+// C ABI of the engine: resident portfolios, queries, and the drop-in
+// get_cuda_model() for the reference's plugin API.
+//
+// Reference boundary replaced (src/05-GPU/monte_carlos_cuda.cu):
+//   :75-163  cuda_simulate  -> rg_run / rg_simulate (this file)
+//   :165-171 get_cuda_model -> get_cuda_model (this file)
+// Contract kept from src/model_interface.h:30 and src/main_runner.c:47-52,
+// 200, 248, 294-295: run_model returns 0 or -1 with a message on stderr,
+// result is zeroed by the caller, S_values is malloc'ed by the model (or
+// left NULL) and freed by the caller.
+//
+// Process-global state: one context per CUDA device (stream, timing events,
+// SM count), created on first use; everything else is owned by the handles.
+#include <cmath>
+#include <climits>
+#include <cstdarg>
+#include <cstdio>
+#include <cstdlib>
+#include <cstring>
+#include <mutex>
+#include <vector>
+
+#include "rg_internal.cuh"
+#include "riskgpu_plugin.h"
+
+namespace rg {
+
+static thread_local char g_err[512] = "";
+
+int set_error(int status, const char *fmt, ...)
+{
+    va_list ap;
+    va_start(ap, fmt);
+    vsnprintf(g_err, sizeof(g_err), fmt, ap);
+    va_end(ap);
+    return status;
+}
+
+struct DevCtx {
+    bool ready = false;
+    int sm_count = 0;
+    cudaStream_t stream = nullptr;
+};
+
+static std::mutex g_mu;
+static DevCtx g_ctx[64];
+
+static int env_flag(const char *name)
+{
+    const char *e = getenv(name);
+    return (e && e[0] && e[0] != '0') ? 1 : 0;
+}
+
+static bool env_contains(const char *name, const char *word)
+{
+    const char *e = getenv(name);
+    return e && strstr(e, word) != nullptr;
+}
+
+// Device context of the current device (created on first use).
+static int get_ctx(DevCtx **out, int *dev_out)
+{
+    int count = 0;
+    if (cudaGetDeviceCount(&count) != cudaSuccess || count <= 0) {
+        cudaGetLastError();
+        return set_error(RG_ERR_NO_DEVICE, "no CUDA device is available");
+    }
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64)
+        return set_error(RG_ERR_NO_DEVICE, "cannot query the current CUDA device");
+    std::lock_guard<std::mutex> lk(g_mu);
+    DevCtx &c = g_ctx[dev];
+    if (!c.ready) {
+        cudaError_t e = cudaDeviceGetAttribute(&c.sm_count, cudaDevAttrMultiProcessorCount, dev);
+        if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&c.stream, cudaStreamNonBlocking);
+        if (e != cudaSuccess)
+            return set_error(RG_ERR_CUDA, "device init failed: %s", cudaGetErrorString(e));
+        c.ready = true;
+    }
+    *out = &c;
+    if (dev_out) *dev_out = dev;
+    return RG_OK;
+}
+
+#define RG_CUDA_TRY(call)                                                                          \
+    do {                                                                                           \
+        cudaError_t e_ = (call);                                                                   \
+        if (e_ != cudaSuccess) {                                                                   \
+            st = set_error(e_ == cudaErrorMemoryAllocation ? RG_ERR_NOMEM : RG_ERR_CUDA,          \
+                           "%s failed: %s", #call, cudaGetErrorString(e_));                      \
+            goto fail;                                                                             \
+        }                                                                                          \
+    } while (0)
+
+static bool all_finite(const double *v, size_t n)
+{
+    for (size_t i = 0; i < n; i++)
+        if (!std::isfinite(v[i])) return false;
+    return true;
+}
+
+// Free-memory admission: refuse an allocation of `need` bytes when it would
+// leave less than RG_MEM_HEADROOM_BYTES free.  RG_FAULT_INJECT=alloc makes
+// every engine allocation fail as if cudaMalloc had (host-side injection).
+static int admit(size_t need)
+{
+    if (env_contains("RG_FAULT_INJECT", "alloc"))
+        return set_error(RG_ERR_NOMEM, "injected allocation failure (RG_FAULT_INJECT=alloc)");
+    const char *h = getenv("RG_MEM_HEADROOM_BYTES");
+    if (h && h[0]) {
+        size_t headroom = (size_t)strtoull(h, nullptr, 10);
+        size_t fr = 0, tot = 0;
+        if (cudaMemGetInfo(&fr, &tot) != cudaSuccess)
+            return set_error(RG_ERR_CUDA, "cudaMemGetInfo failed");
+        if (fr < need || fr - need < headroom)
+            return set_error(RG_ERR_ADMISSION,
+                             "admission refused: %zu bytes requested, %zu free, headroom %zu", need,
+                             fr, headroom);
+    }
+    return RG_OK;
+}
+
+static void portfolio_free(Portfolio *p)
+{
+    if (!p) return;
+    cudaFree(p->d_L64);
+    cudaFree(p->d_mu64);
+    cudaFree(p->d_Lp);
+    cudaFree(p->d_w32);
+    cudaFree(p->d_aux);
+    cudaFree(p->d_info);
+    delete p;
+}
+
+static int validate_query(const Portfolio *p, const rg_query *q)
+{
+    if (!q) return set_error(RG_ERR_INVALID, "query is NULL");
+    if (q->n_paths < 1) return set_error(RG_ERR_INVALID, "n_paths must be >= 1 (got %lld)", (long long)q->n_paths);
+    if (q->horizon < 1) return set_error(RG_ERR_INVALID, "horizon must be >= 1 (got %d)", q->horizon);
+    if (!std::isfinite(q->x)) return set_error(RG_ERR_INVALID, "x must be finite");
+    if (!std::isfinite(q->port_threshold)) return set_error(RG_ERR_INVALID, "port_threshold must be finite");
+    if (q->rng != RG_RNG_PHILOX && q->rng != RG_RNG_XORWOW_REF)
+        return set_error(RG_ERR_INVALID, "unknown rng layout %d", q->rng);
+    if (q->precision < RG_PREC_FP32 || q->precision > RG_PREC_AUTO)
+        return set_error(RG_ERR_INVALID, "unknown precision %d", q->precision);
+    if (!(q->var_level >= 0.0 && q->var_level < 1.0))
+        return set_error(RG_ERR_INVALID, "var_level must be in [0, 1)");
+    if (p && p->n > plain_small_max_n())
+        return set_error(RG_ERR_UNSUPPORTED, "N = %d exceeds this kernel's limit %d", p->n,
+                         plain_small_max_n());
+    return RG_OK;
+}
+
+static PlainArgs make_args(const Portfolio *p, const rg_query *q, unsigned long long *d_counts)
+{
+    PlainArgs a;
+    memset(&a, 0, sizeof(a));
+    a.Lp = reinterpret_cast<const float4 *>(p->d_Lp);
+    a.mu64 = p->d_mu64;
+    a.w = p->d_w32;
+    a.n = p->n;
+    a.horizon = q->horizon;
+    a.n_paths = q->n_paths;
+    a.path0 = q->path_offset;
+    a.seed = q->seed;
+    a.keys = philox_round_keys(q->seed);
+    a.neg_x = (float)(-q->x);
+    a.port_thr = (float)q->port_threshold;
+    a.k = q->k;
+    a.has_w = p->has_w;
+    a.s_values = q->d_s_values;
+    a.port_values = q->d_port_values;
+    a.counts = d_counts;
+    return a;
+}
+
+} // namespace rg
+
+using namespace rg;
+
+extern "C" {
+
+int rg_abi_version(void) { return RG_ABI_VERSION; }
+
+const char *rg_status_string(int status)
+{
+    switch (status) {
+    case RG_OK: return "ok";
+    case RG_ERR_INVALID: return "invalid argument";
+    case RG_ERR_NOT_PD: return "covariance not positive definite";
+    case RG_ERR_CUDA: return "CUDA error";
+    case RG_ERR_NOMEM: return "out of memory";
+    case RG_ERR_UNSUPPORTED: return "unsupported";
+    case RG_ERR_ADMISSION: return "admission refused (memory headroom)";
+    case RG_ERR_NO_DEVICE: return "no CUDA device";
+    case RG_ERR_TIMEOUT: return "device wait timed out";
+    case RG_ERR_BUSY: return "busy";
+    default: return "unknown status";
+    }
+}
+
+const char *rg_last_error(void) { return g_err; }
+
+int rg_device_count(void)
+{
+    int c = 0;
+    if (cudaGetDeviceCount(&c) != cudaSuccess) {
+        cudaGetLastError();
+        return 0;
+    }
+    return c;
+}
+
+void rg_estimator_stats(int64_t count, int64_t M, double *p, double *se, double *lo, double *hi)
+{
+    const double P = (M > 0) ? (double)count / (double)M : NAN;
+    const double S = std::sqrt(P * (1.0 - P) / (double)M);
+    const double margin = 1.96 * S;
+    if (p) *p = P;
+    if (se) *se = S;
+    if (lo) *lo = std::fmax(0.0, P - margin);
+    if (hi) *hi = std::fmin(1.0, P + margin);
+}
+
+int64_t rg_tail_count(int64_t M, double level)
+{
+    double t = std::ceil((1.0 - level) * (double)M - 1e-9);
+    if (t < 1.0) t = 1.0;
+    if (t > (double)M) t = (double)M;
+    return (int64_t)t;
+}
+
+int rg_portfolio_create(int32_t n, const double *mu, const double *sigma, int64_t ld,
+                        const double *weights, int32_t flags, rg_portfolio **out)
+{
+    if (!out) return set_error(RG_ERR_INVALID, "out is NULL");
+    *out = nullptr;
+    if (n < 1) return set_error(RG_ERR_INVALID, "N must be >= 1 (got %d)", n);
+    if (n > cholesky_max_n()) return set_error(RG_ERR_UNSUPPORTED, "N = %d exceeds %d", n, cholesky_max_n());
+    if (!mu || !sigma) return set_error(RG_ERR_INVALID, "mu and sigma must not be NULL");
+    if (ld < n) return set_error(RG_ERR_INVALID, "leading dimension %lld < N", (long long)ld);
+    const bool dev_in = (flags & RG_INPUT_DEVICE) != 0;
+    if (!dev_in) {
+        if (!all_finite(mu, (size_t)n)) return set_error(RG_ERR_INVALID, "mu has a NaN or Inf");
+        if (weights && !all_finite(weights, (size_t)n)) return set_error(RG_ERR_INVALID, "weights have a NaN or Inf");
+        for (int i = 0; i < n; i++)
+            if (!all_finite(sigma + (size_t)i * ld, (size_t)i + 1))
+                return set_error(RG_ERR_INVALID, "Sigma has a NaN or Inf in row %d", i);
+    }
+    DevCtx *ctx;
+    int dev;
+    int st = get_ctx(&ctx, &dev);
+    if (st) return st;
+    const size_t nn = (size_t)n * n;
+    const size_t need = nn * 8 * (dev_in ? 1 : 2) + (size_t)n * 24 + (size_t)packed_len(n) * 4 + 64;
+    st = admit(need);
+    if (st) return st;
+
+    Portfolio *p = new Portfolio();
+    p->n = n;
+    p->has_w = weights ? 1 : 0;
+    p->device = dev;
+    double *dA = nullptr, *dW = nullptr;
+    const double *A = sigma, *W = weights, *MU = mu;
+    long long lda = ld;
+    int info = 0;
+    double aux[2] = {0, 0};
+    cudaEvent_t e0 = nullptr, e1 = nullptr;
+    cudaStream_t s = ctx->stream;
+    RG_CUDA_TRY(cudaMalloc(&p->d_L64, nn * sizeof(double)));
+    RG_CUDA_TRY(cudaMalloc(&p->d_mu64, (size_t)n * sizeof(double)));
+    RG_CUDA_TRY(cudaMalloc(&p->d_Lp, (size_t)packed_len(n) * sizeof(float)));
+    RG_CUDA_TRY(cudaMalloc(&p->d_w32, (size_t)n * sizeof(float)));
+    RG_CUDA_TRY(cudaMalloc(&p->d_aux, 2 * sizeof(double)));
+    RG_CUDA_TRY(cudaMalloc(&p->d_info, sizeof(int)));
+    if (!dev_in) {
+        RG_CUDA_TRY(cudaMalloc(&dA, nn * sizeof(double)));
+        RG_CUDA_TRY(cudaMemcpy2DAsync(dA, (size_t)n * sizeof(double), sigma, (size_t)ld * sizeof(double),
+                                      (size_t)n * sizeof(double), (size_t)n, cudaMemcpyHostToDevice, s));
+        RG_CUDA_TRY(cudaMemcpyAsync(p->d_mu64, mu, (size_t)n * sizeof(double), cudaMemcpyHostToDevice, s));
+        if (weights) {
+            RG_CUDA_TRY(cudaMalloc(&dW, (size_t)n * sizeof(double)));
+            RG_CUDA_TRY(cudaMemcpyAsync(dW, weights, (size_t)n * sizeof(double), cudaMemcpyHostToDevice, s));
+        }
+        A = dA;
+        W = dW;
+        MU = p->d_mu64;
+        lda = n;
+    } else {
+        RG_CUDA_TRY(cudaMemcpyAsync(p->d_mu64, mu, (size_t)n * sizeof(double), cudaMemcpyDeviceToDevice, s));
+        MU = p->d_mu64;
+    }
+    RG_CUDA_TRY(cudaEventCreate(&e0));
+    RG_CUDA_TRY(cudaEventCreate(&e1));
+    RG_CUDA_TRY(cudaEventRecord(e0, s));
+    RG_CUDA_TRY(launch_cholesky(A, lda, n, W, MU, p->d_L64, p->d_Lp, p->d_w32, p->d_aux, p->d_info, s));
+    RG_CUDA_TRY(cudaEventRecord(e1, s));
+    RG_CUDA_TRY(cudaMemcpyAsync(&info, p->d_info, sizeof(int), cudaMemcpyDeviceToHost, s));
+    RG_CUDA_TRY(cudaMemcpyAsync(aux, p->d_aux, sizeof(aux), cudaMemcpyDeviceToHost, s));
+    RG_CUDA_TRY(cudaStreamSynchronize(s));
+    cudaEventElapsedTime(&p->ms_chol, e0, e1);
+    if (info == -1) {
+        st = set_error(RG_ERR_INVALID, "mu, weights or Sigma hold a NaN or Inf");
+        goto fail;
+    }
+    if (info != 0) {
+        st = set_error(RG_ERR_NOT_PD, "Cholesky failed: Sigma is not positive definite (pivot %d)", info - 1);
+        goto fail;
+    }
+    p->wsw = aux[0];
+    p->wmu = aux[1];
+    cudaFree(dA);
+    cudaFree(dW);
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    *out = reinterpret_cast<rg_portfolio *>(p);
+    return RG_OK;
+fail:
+    cudaStreamSynchronize(s);
+    cudaFree(dA);
+    cudaFree(dW);
+    if (e0) cudaEventDestroy(e0);
+    if (e1) cudaEventDestroy(e1);
+    portfolio_free(p);
+    return st;
+}
+
+int rg_portfolio_destroy(rg_portfolio *h)
+{
+    if (!h) return RG_OK;
+    portfolio_free(reinterpret_cast<Portfolio *>(h));
+    return RG_OK;
+}
+
+int rg_portfolio_info_get(const rg_portfolio *h, rg_portfolio_info *out)
+{
+    if (!h || !out) return set_error(RG_ERR_INVALID, "NULL argument");
+    const Portfolio *p = reinterpret_cast<const Portfolio *>(h);
+    out->n_assets = p->n;
+    out->has_weights = p->has_w;
+    out->d_L = p->d_L64;
+    out->d_packed = p->d_Lp;
+    out->wsw = p->wsw;
+    out->wmu = p->wmu;
+    out->ms_cholesky = p->ms_chol;
+    return RG_OK;
+}
+
+int rg_portfolio_factor(const rg_portfolio *h, double *L_host)
+{
+    if (!h || !L_host) return set_error(RG_ERR_INVALID, "NULL argument");
+    const Portfolio *p = reinterpret_cast<const Portfolio *>(h);
+    cudaError_t e = cudaMemcpy(L_host, p->d_L64, (size_t)p->n * p->n * sizeof(double), cudaMemcpyDeviceToHost);
+    if (e != cudaSuccess) return set_error(RG_ERR_CUDA, "copy of L failed: %s", cudaGetErrorString(e));
+    return RG_OK;
+}
+
+int rg_launch_counts(const rg_portfolio *h, const rg_query *q, unsigned long long *d_counts, void *stream)
+{
+    if (!h || !d_counts) return set_error(RG_ERR_INVALID, "NULL argument");
+    const Portfolio *p = reinterpret_cast<const Portfolio *>(h);
+    int st = validate_query(p, q);
+    if (st) return st;
+    DevCtx *ctx;
+    st = get_ctx(&ctx, nullptr);
+    if (st) return st;
+    cudaStream_t s = stream ? (cudaStream_t)stream : ctx->stream;
+    cudaError_t e = cudaMemsetAsync(d_counts, 0, 2 * sizeof(unsigned long long), s);
+    if (e == cudaSuccess) e = launch_plain_small(make_args(p, q, d_counts), q->rng, ctx->sm_count, s);
+    if (e != cudaSuccess) return set_error(RG_ERR_CUDA, "launch failed: %s", cudaGetErrorString(e));
+    return RG_OK;
+}
+
+int rg_simulate(const rg_portfolio *h, const rg_query *q, rg_result *out, void *stream)
+{
+    if (!h || !out) return set_error(RG_ERR_INVALID, "NULL argument");
+    const Portfolio *p = reinterpret_cast<const Portfolio *>(h);
+    int st = validate_query(p, q);
+    if (st) return st;
+    DevCtx *ctx;
+    st = get_ctx(&ctx, nullptr);
+    if (st) return st;
+    cudaStream_t s = stream ? (cudaStream_t)stream : ctx->stream;
+    unsigned long long *d_counts = nullptr;
+    unsigned long long counts[2] = {0, 0};
+    cudaEvent_t e0 = nullptr, e1 = nullptr;
+    float ms = 0.f;
+    st = admit(64);
+    if (st) return st;
+    RG_CUDA_TRY(cudaMallocAsync((void **)&d_counts, 2 * sizeof(unsigned long long), s));
+    RG_CUDA_TRY(cudaMemsetAsync(d_counts, 0, 2 * sizeof(unsigned long long), s));
+    RG_CUDA_TRY(cudaEventCreate(&e0));
+    RG_CUDA_TRY(cudaEventCreate(&e1));
+    RG_CUDA_TRY(cudaEventRecord(e0, s));
+    RG_CUDA_TRY(launch_plain_small(make_args(p, q, d_counts), q->rng, ctx->sm_count, s));
+    RG_CUDA_TRY(cudaEventRecord(e1, s));
+    RG_CUDA_TRY(cudaMemcpyAsync(counts, d_counts, sizeof(counts), cudaMemcpyDeviceToHost, s));
+    RG_CUDA_TRY(cudaFreeAsync(d_counts, s));
+    d_counts = nullptr;
+    RG_CUDA_TRY(cudaStreamSynchronize(s));
+    cudaEventElapsedTime(&ms, e0, e1);
+    memset(out, 0, sizeof(*out));
+    out->n_paths = q->n_paths;
+    out->crash_count = (int64_t)counts[0];
+    out->breach_count = (int64_t)counts[1];
+    rg_estimator_stats(out->crash_count, q->n_paths, &out->p_crash, &out->se_crash, &out->ci_lower,
+                       &out->ci_upper);
+    rg_estimator_stats(out->breach_count, q->n_paths, &out->p_breach, &out->se_breach, nullptr, nullptr);
+    out->var = NAN;
+    out->cvar = NAN;
+    out->tail_count = 0;
+    out->var_passes = 0;
+    out->ms_device = ms;
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    return RG_OK;
+fail:
+    cudaStreamSynchronize(s);
+    if (d_counts) cudaFree(d_counts);
+    if (e0) cudaEventDestroy(e0);
+    if (e1) cudaEventDestroy(e1);
+    return st;
+}
+
+int rg_run(int32_t n, const double *mu, const double *sigma, int64_t ld, const double *weights,
+           const rg_query *q, rg_result *out)
+{
+    int st = validate_query(nullptr, q);
+    if (st) return st;
+    if (n > plain_small_max_n())
+        return set_error(RG_ERR_UNSUPPORTED, "N = %d exceeds this kernel's limit %d", n, plain_small_max_n());
+    rg_portfolio *h = nullptr;
+    st = rg_portfolio_create(n, mu, sigma, ld, weights, 0, &h);
+    if (st) return st;
+    st = rg_simulate(h, q, out, nullptr);
+    rg_portfolio_destroy(h);
+    return st;
+}
+
+// ------------------------------------------------------------- drop-in
+int cuda_simulate(MonteCarloParams *params, MonteCarloResult *result)
+{
+    if (!params || !result) {
+        fprintf(stderr, "Error: cuda_simulate called with NULL params or result\n");
+        return -1;
+    }
+    printf("Starting CUDA Monte Carlo simulation with M = %d trials...\n", params->M);
+    const int n = params->N;
+    if (n < 1 || params->M < 1 || !params->mu || !params->Sigma || !params->mu->data ||
+        !params->Sigma->data) {
+        fprintf(stderr, "Error: invalid parameters (N=%d, M=%d)\n", n, params->M);
+        return -1;
+    }
+    if ((int)params->mu->size != n || (int)params->Sigma->size1 != n || (int)params->Sigma->size2 != n) {
+        fprintf(stderr, "Error: mu/Sigma sizes do not match N=%d\n", n);
+        return -1;
+    }
+    std::vector<double> mu((size_t)n);
+    for (int i = 0; i < n; i++) mu[(size_t)i] = params->mu->data[(size_t)i * params->mu->stride];
+
+    rg_query q;
+    memset(&q, 0, sizeof(q));
+    q.n_paths = params->M;
+    q.seed = (uint64_t)params->random_seed;
+    q.horizon = 1;
+    q.k = params->k;
+    q.x = params->x;
+    q.port_threshold = 0.0;
+    q.rng = env_contains("RG_RNG", "xorwow") ? RG_RNG_XORWOW_REF : RG_RNG_PHILOX;
+    q.precision = RG_PREC_AUTO;
+    q.var_level = 0.0;
+    const bool want_s = env_flag("RG_MATERIALIZE_S") != 0;
+
+    rg_portfolio *h = nullptr;
+    rg_result r;
+    int *d_s = nullptr;
+    int st = rg_portfolio_create(n, mu.data(), params->Sigma->data, (int64_t)params->Sigma->tda, nullptr, 0, &h);
+    if (st == RG_OK && want_s) {
+        if (cudaMalloc(&d_s, (size_t)params->M * sizeof(int)) != cudaSuccess) {
+            st = set_error(RG_ERR_NOMEM, "cudaMalloc of S_values failed");
+        }
+        q.d_s_values = d_s;
+    }
+    if (st == RG_OK) st = rg_simulate(h, &q, &r, nullptr);
+    if (st == RG_OK && want_s) {
+        result->S_values = (int *)malloc((size_t)params->M * sizeof(int));
+        if (!result->S_values ||
+            cudaMemcpy(result->S_values, d_s, (size_t)params->M * sizeof(int), cudaMemcpyDeviceToHost) != cudaSuccess)
+            st = set_error(RG_ERR_NOMEM, "copy of S_values failed");
+    }
+    if (d_s) cudaFree(d_s);
+    rg_portfolio_destroy(h);
+    if (st != RG_OK) {
+        fprintf(stderr, "Error: CUDA model failed: %s (%s)\n", rg_status_string(st), rg_last_error());
+        return -1;
+    }
+    result->count = r.crash_count > INT_MAX ? INT_MAX : (int)r.crash_count;
+    // statistics from the exact 64-bit count (.cu:146-150)
+    result->P_hat = r.p_crash;
+    result->std_error = r.se_crash;
+    result->ci_lower = r.ci_lower;
+    result->ci_upper = r.ci_upper;
+    printf("CUDA Simulation complete\n");
+    return 0;
+}
+
+ModelFunctions get_cuda_model(void)
+{
+    ModelFunctions m;
+    m.name = "cuda";
+    m.run_model = cuda_simulate;
+    return m;
+}
+
+} // extern "C"

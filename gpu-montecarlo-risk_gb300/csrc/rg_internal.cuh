@@ -1,0 +1,151 @@
+// Internal declarations shared by the engine's translation units.
+//
+// Device helpers:
+//   rg_philox       Philox4x32-10 (Salmon et al., SC'11): 10 rounds of two
+//                   32x32->64 multiplies with the published multipliers and
+//                   Weyl key increments.  Round keys are precomputed on the
+//                   host (they depend only on the seed).
+//   rg_box_muller   Box-Muller (Box & Muller 1958) on two 32-bit words:
+//                   u = w 2^-32 + 2^-33 in (0, 1], r = sqrt(-2 ln u_a),
+//                   t = 2 pi (u_b - 1/2), (z0, z1) = (r cos t, r sin t), using
+//                   the hardware approximate lg2/sqrt/sin/cos (PTX *.approx).
+#pragma once
+
+#include <cstdint>
+#include <cuda_runtime.h>
+
+#include "riskgpu.h"
+
+namespace rg {
+
+// ---------------------------------------------------------------- device
+struct PhiloxKeys {
+    uint32_t k0[10];
+    uint32_t k1[10];
+};
+
+inline PhiloxKeys philox_round_keys(uint64_t seed)
+{
+    PhiloxKeys k;
+    uint32_t a = (uint32_t)seed, b = (uint32_t)(seed >> 32);
+    for (int r = 0; r < 10; r++) {
+        k.k0[r] = a;
+        k.k1[r] = b;
+        a += 0x9E3779B9u;
+        b += 0xBB67AE85u;
+    }
+    return k;
+}
+
+__device__ __forceinline__ uint4 rg_philox(uint4 c, const PhiloxKeys &k)
+{
+#pragma unroll
+    for (int r = 0; r < 10; r++) {
+        const uint64_t p0 = (uint64_t)0xD2511F53u * c.x;
+        const uint64_t p1 = (uint64_t)0xCD9E8D57u * c.z;
+        const uint32_t hi0 = (uint32_t)(p0 >> 32), lo0 = (uint32_t)p0;
+        const uint32_t hi1 = (uint32_t)(p1 >> 32), lo1 = (uint32_t)p1;
+        c = make_uint4(hi1 ^ c.y ^ k.k0[r], lo1, hi0 ^ c.w ^ k.k1[r], lo0);
+    }
+    return c;
+}
+
+__device__ __forceinline__ float rg_lg2_approx(float x)
+{
+    float y;
+    asm("lg2.approx.ftz.f32 %0, %1;" : "=f"(y) : "f"(x));
+    return y;
+}
+__device__ __forceinline__ float rg_sqrt_approx(float x)
+{
+    float y;
+    asm("sqrt.approx.ftz.f32 %0, %1;" : "=f"(y) : "f"(x));
+    return y;
+}
+__device__ __forceinline__ float rg_sin_approx(float x)
+{
+    float y;
+    asm("sin.approx.ftz.f32 %0, %1;" : "=f"(y) : "f"(x));
+    return y;
+}
+__device__ __forceinline__ float rg_cos_approx(float x)
+{
+    float y;
+    asm("cos.approx.ftz.f32 %0, %1;" : "=f"(y) : "f"(x));
+    return y;
+}
+
+__device__ __forceinline__ float rg_uniform(uint32_t w)
+{
+    return __fmaf_rn(__uint2float_rn(w), 0x1p-32f, 0x1p-33f);
+}
+
+__device__ __forceinline__ void rg_box_muller(uint32_t a, uint32_t b, float &z0, float &z1)
+{
+    const float ua = rg_uniform(a);
+    const float ub = rg_uniform(b);
+    // -2 ln(u) = -2 ln(2) log2(u)
+    const float r = rg_sqrt_approx(-1.3862943611198906f * rg_lg2_approx(ua));
+    const float t = 6.283185307179586f * (ub - 0.5f);
+    z0 = r * rg_cos_approx(t);
+    z1 = r * rg_sin_approx(t);
+}
+
+// Packed FP32 lower-triangular rows: row i holds L[i][0..i] zero-padded to
+// a multiple of 4 floats, so every row starts on a 16-byte boundary.
+// offset(i) = sum_{r<i} 4 ceil((r+1)/4) = 4 (a+1)(2a+b) for i = 4a+b.
+__host__ __device__ constexpr int packed_row_offset(int i)
+{
+    return 4 * (i / 4 + 1) * (2 * (i / 4) + (i % 4));
+}
+__host__ __device__ constexpr int packed_len(int n) { return packed_row_offset(n); }
+
+// ---------------------------------------------------------------- host
+struct Portfolio {
+    int n = 0;
+    int has_w = 0;
+    int device = 0;
+    double *d_L64 = nullptr;   // n x n row-major, zero upper
+    double *d_mu64 = nullptr;  // n
+    float *d_Lp = nullptr;     // packed rows (packed_len(n) floats)
+    float *d_w32 = nullptr;    // n (zeros when no weights)
+    double *d_aux = nullptr;   // [2]: w^T Sigma w, w.mu
+    int *d_info = nullptr;
+    double wsw = 0.0, wmu = 0.0;
+    float ms_chol = 0.f;
+};
+
+// Arguments of the fused counting kernels.
+struct PlainArgs {
+    const float4 *Lp;
+    const double *mu64;
+    const float *w;
+    int n;
+    int horizon;
+    long long n_paths;
+    unsigned long long path0;
+    unsigned long long seed;
+    PhiloxKeys keys;
+    float neg_x;
+    float port_thr;
+    int k;
+    int has_w;
+    int *s_values;
+    float *port_values;
+    unsigned long long *counts; // [2]
+};
+
+// Launchers (rg_mc_plain.cu).  Return cudaSuccess or the launch error.
+cudaError_t launch_plain_small(const PlainArgs &a, int rng, int sm_count, cudaStream_t s);
+int plain_small_max_n();
+
+// Cholesky (rg_cholesky.cu): factor, pack and portfolio moments.
+cudaError_t launch_cholesky(const double *A, long long lda, int n, const double *w,
+                            const double *mu, double *L64, float *Lp, float *w32, double *aux,
+                            int *info, cudaStream_t s);
+int cholesky_max_n();
+
+// Error helpers (rg_capi.cu).
+int set_error(int status, const char *fmt, ...);
+
+} // namespace rg

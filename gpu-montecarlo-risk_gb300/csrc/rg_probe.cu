@@ -1,0 +1,104 @@
+// Measured peaks for the roofline of the fused kernels.
+//
+// The fused counting kernels are bound by instruction issue on the FP32 /
+// integer / special-function pipes, not by HBM or tensor cores, so their
+// roofline denominators are measured here on the device that runs them:
+//   probe_ffma     independent FP32 fused multiply-add chains: FP32 FLOP/s
+//   probe_normals  the engine's Philox4x32-10 + Box-Muller normal generator
+//                  alone (no contraction): normals/s
+// Both fill every SM (grid = SMs x resident CTAs) and are timed with CUDA
+// events on the caller's stream.
+#include <cstdio>
+#include "rg_internal.cuh"
+
+namespace rg {
+
+static constexpr int kProbeThreads = 256;
+
+__global__ void __launch_bounds__(kProbeThreads) probe_ffma_kernel(int iters, float seed, float *sink)
+{
+    float a[8];
+#pragma unroll
+    for (int c = 0; c < 8; c++) a[c] = seed + 1e-3f * (float)(threadIdx.x + c);
+    const float b = 0.99999f, d = 1e-6f;
+    for (int i = 0; i < iters; i++) {
+#pragma unroll
+        for (int u = 0; u < 16; u++) {
+#pragma unroll
+            for (int c = 0; c < 8; c++) a[c] = fmaf(a[c], b, d);
+        }
+    }
+    float s = 0.f;
+#pragma unroll
+    for (int c = 0; c < 8; c++) s += a[c];
+    if (s == -1.0f) sink[0] = s; // never true for these inputs; keeps the chains live
+}
+
+__global__ void __launch_bounds__(kProbeThreads) probe_normals_kernel(int iters, PhiloxKeys keys, float *sink)
+{
+    const uint32_t path = blockIdx.x * blockDim.x + threadIdx.x;
+    float acc = 0.f;
+    for (int i = 0; i < iters; i++) {
+        const uint4 r = rg_philox(make_uint4((uint32_t)i, 0u, path, 0u), keys);
+        float z0, z1, z2, z3;
+        rg_box_muller(r.x, r.y, z0, z1);
+        rg_box_muller(r.z, r.w, z2, z3);
+        acc += (z0 + z1) + (z2 + z3);
+    }
+    if (acc == -12345.f) sink[0] = acc;
+}
+
+} // namespace rg
+
+using namespace rg;
+
+extern "C" int rg_probe_peaks(rg_peaks *out, void *stream)
+{
+    if (!out) return set_error(RG_ERR_INVALID, "out is NULL");
+    int dev = 0, sms = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess ||
+        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess) {
+        cudaGetLastError();
+        return set_error(RG_ERR_NO_DEVICE, "no CUDA device is available");
+    }
+    cudaStream_t s = (cudaStream_t)stream;
+    float *sink = nullptr;
+    cudaEvent_t e0, e1;
+    if (cudaMalloc(&sink, 16) != cudaSuccess) return set_error(RG_ERR_NOMEM, "probe sink alloc failed");
+    cudaEventCreate(&e0);
+    cudaEventCreate(&e1);
+    int per_sm = 0;
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, probe_ffma_kernel, kProbeThreads, 0);
+    const int grid_f = sms * (per_sm > 0 ? per_sm : 1);
+    const int iters_f = 4096;
+    probe_ffma_kernel<<<grid_f, kProbeThreads, 0, s>>>(64, 1.0f, sink); // warm-up
+    cudaEventRecord(e0, s);
+    probe_ffma_kernel<<<grid_f, kProbeThreads, 0, s>>>(iters_f, 1.0f, sink);
+    cudaEventRecord(e1, s);
+    cudaEventSynchronize(e1);
+    float ms_f = 0.f;
+    cudaEventElapsedTime(&ms_f, e0, e1);
+
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, probe_normals_kernel, kProbeThreads, 0);
+    const int grid_n = sms * (per_sm > 0 ? per_sm : 1);
+    const int iters_n = 2048;
+    PhiloxKeys keys = philox_round_keys(0x5eedULL);
+    probe_normals_kernel<<<grid_n, kProbeThreads, 0, s>>>(32, keys, sink);
+    cudaEventRecord(e0, s);
+    probe_normals_kernel<<<grid_n, kProbeThreads, 0, s>>>(iters_n, keys, sink);
+    cudaEventRecord(e1, s);
+    cudaEventSynchronize(e1);
+    float ms_n = 0.f;
+    cudaEventElapsedTime(&ms_n, e0, e1);
+    cudaError_t e = cudaGetLastError();
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    cudaFree(sink);
+    if (e != cudaSuccess) return set_error(RG_ERR_CUDA, "probe failed: %s", cudaGetErrorString(e));
+    const double flops = 2.0 * 8 * 16 * (double)iters_f * grid_f * kProbeThreads;
+    const double normals = 4.0 * (double)iters_n * grid_n * kProbeThreads;
+    out->fp32_tflops = flops / (ms_f * 1e-3) / 1e12;
+    out->normals_per_s = normals / (ms_n * 1e-3);
+    out->sm_count = sms;
+    return RG_OK;
+}

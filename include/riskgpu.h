@@ -1,0 +1,160 @@
+/*
+ * riskgpu -- GB300 (sm_103a) Monte Carlo portfolio-risk engine, C ABI.
+ *
+ * Plain C types and pointers only.  Every entry point returns an rg_status
+ * (0 = success, negative = error class); rg_last_error() gives the message
+ * of the calling thread's last failure.  Streams are passed as `void *`
+ * holding a cudaStream_t (NULL = the engine's own stream).
+ *
+ * Model (the reference's, src/01-python-serial/python_serial.py:3-7 and
+ * src/05-GPU/monte_carlos_cuda.cu:23-72, extended by portfolio weights and
+ * a horizon): for each path p,
+ *     Zsum = sum_{d<H} Z_d,  Z_d ~ N(0, I_N)
+ *     R    = H mu + L Zsum,  L L^T = Sigma (FP64 Cholesky on the GPU)
+ *     S    = #{ i : R_i < -x }            crash count   (reference)
+ *     crash  if S >= k                     (reference's extreme event)
+ *     breach if w.R < port_threshold       (portfolio extension)
+ * plus VaR / CVaR of the loss -w.R.  Counts are exact 64-bit integers.
+ */
+#ifndef RISKGPU_H
+#define RISKGPU_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define RG_ABI_VERSION 1
+
+typedef enum {
+    RG_OK = 0,
+    RG_ERR_INVALID = -1,     /* bad argument (sizes, NaN/Inf inputs, null pointers) */
+    RG_ERR_NOT_PD = -2,      /* covariance not positive definite (Cholesky pivot <= 0) */
+    RG_ERR_CUDA = -3,        /* a CUDA runtime call or kernel failed */
+    RG_ERR_NOMEM = -4,       /* device or host allocation failed */
+    RG_ERR_UNSUPPORTED = -5, /* valid request this build cannot serve (size limits) */
+    RG_ERR_ADMISSION = -6,   /* refused: not enough free device memory headroom */
+    RG_ERR_NO_DEVICE = -7,   /* no usable CUDA device */
+    RG_ERR_TIMEOUT = -8,     /* a bounded device wait ran out (error word set on device) */
+    RG_ERR_BUSY = -9         /* queue full / handle in use */
+} rg_status;
+
+/* Normal-draw layout. */
+typedef enum {
+    /* Counter-based Philox4x32-10, key = seed, counter = (block, 0, path):
+     * the same 32-bit stream as cuRAND's curand_init(seed, path, 0) for
+     * curandStatePhilox4_32_10_t.  Normals by Box-Muller in FP32. */
+    RG_RNG_PHILOX = 0,
+    /* The reference kernel's own stream (monte_carlos_cuda.cu:30-31,45-47):
+     * curand_init(seed, path, 0, &curandStateXORWOW_t) then
+     * curand_normal_double per asset, rounded to FP32. */
+    RG_RNG_XORWOW_REF = 1
+} rg_rng_layout;
+
+/* Arithmetic of the correlation step R = H mu + L Zsum. */
+typedef enum {
+    RG_PREC_FP32 = 0,   /* FP32 FMA cores (the plain fused kernel) */
+    RG_PREC_BF16X3 = 1, /* tcgen05 tensor cores, BF16 hi+lo split of Z and L, FP32 accumulate */
+    RG_PREC_AUTO = 2    /* the engine picks by asset count */
+} rg_precision;
+
+/* Flags for rg_portfolio_create. */
+#define RG_INPUT_DEVICE 0x1 /* mu, sigma, weights are device pointers */
+
+typedef struct rg_portfolio rg_portfolio; /* opaque: device-resident factor */
+
+typedef struct {
+    int32_t n_assets;
+    int32_t has_weights;
+    const double *d_L;      /* device, row-major n x n FP64, zero upper triangle */
+    const void *d_packed;   /* device, FP32 packed lower rows (engine layout) */
+    double wsw;             /* w^T Sigma w (daily variance of the portfolio return) */
+    double wmu;             /* w . mu */
+    float ms_cholesky;      /* device time of the Cholesky at creation */
+} rg_portfolio_info;
+
+typedef struct {
+    int64_t n_paths;        /* M >= 1 */
+    uint64_t path_offset;   /* first path index (restartable / shardable ranges) */
+    uint64_t seed;
+    int32_t horizon;        /* H >= 1 days, draws summed */
+    int32_t k;              /* crash count threshold (S >= k) */
+    double x;               /* asset crash threshold, R_i < -x */
+    double port_threshold;  /* portfolio breach, w.R < port_threshold */
+    int32_t rng;            /* rg_rng_layout */
+    int32_t precision;      /* rg_precision */
+    double var_level;       /* e.g. 0.99; 0 disables VaR/CVaR */
+    int32_t *d_s_values;    /* optional device output [n_paths]: S per path */
+    float *d_port_values;   /* optional device output [n_paths]: w.R per path */
+} rg_query;
+
+typedef struct {
+    int64_t n_paths;
+    int64_t crash_count;    /* #{S >= k} */
+    int64_t breach_count;   /* #{w.R < port_threshold} */
+    double p_crash, se_crash, ci_lower, ci_upper; /* estimator statistics (reference A8) */
+    double p_breach, se_breach;
+    double var, cvar;       /* loss quantile / tail mean at var_level */
+    int64_t tail_count;     /* number of paths in the VaR tail */
+    int32_t var_passes;     /* 1 = single pass, 2 = band missed and a second pass ran */
+    float ms_device;        /* device time of the simulation kernels */
+} rg_result;
+
+/* ---------------- library ---------------- */
+int rg_abi_version(void);
+const char *rg_status_string(int status);
+const char *rg_last_error(void);
+/* Number of CUDA devices visible (0 when none); never fails. */
+int rg_device_count(void);
+
+/* ---------------- resident portfolios ---------------- */
+/* Uploads mu [n], sigma [n x n, leading dimension ld], weights [n] (nullable)
+ * and factors sigma in FP64 on the GPU.  Replaces the host Cholesky and the
+ * flatten/copy of the reference wrapper (monte_carlos_cuda.cu:84-122). */
+int rg_portfolio_create(int32_t n, const double *mu, const double *sigma, int64_t ld,
+                        const double *weights, int32_t flags, rg_portfolio **out);
+int rg_portfolio_destroy(rg_portfolio *p);
+int rg_portfolio_info_get(const rg_portfolio *p, rg_portfolio_info *out);
+/* Copies the FP64 factor L (row-major, zero upper) to host memory. */
+int rg_portfolio_factor(const rg_portfolio *p, double *L_host);
+
+/* ---------------- simulation ---------------- */
+/* Runs one query to completion and fills `out` (replaces the kernel launch,
+ * copy-back and statistics of monte_carlos_cuda.cu:124-150). */
+int rg_simulate(const rg_portfolio *p, const rg_query *q, rg_result *out, void *stream);
+/* Enqueues only the fused counting kernel on `stream`: d_counts (device,
+ * 2 x uint64: crash, breach) are zeroed and accumulated; no host sync, no
+ * VaR.  For callers that keep inputs and outputs resident. */
+int rg_launch_counts(const rg_portfolio *p, const rg_query *q, unsigned long long *d_counts,
+                     void *stream);
+
+/* One-shot from host buffers: create, simulate, destroy. */
+int rg_run(int32_t n, const double *mu, const double *sigma, int64_t ld, const double *weights,
+           const rg_query *q, rg_result *out);
+
+/* Estimator statistics shared by every back-end of the reference
+ * (monte_carlos_cuda.cu:146-150): p = count/M, se = sqrt(p(1-p)/M),
+ * 95% CI p -+ 1.96 se clamped to [0,1]. */
+void rg_estimator_stats(int64_t count, int64_t M, double *p, double *se, double *lo, double *hi);
+
+/* VaR tail size used by the engine: ceil((1-level) M), clamped to [1, M]. */
+int64_t rg_tail_count(int64_t M, double level);
+
+/* ---------------- measurement ---------------- */
+/* Roofline denominators of the fused kernels, measured on the current
+ * device with micro-kernels timed by CUDA events on `stream`: FP32 FMA
+ * throughput and the engine's normal-generation throughput.  (No
+ * counterpart in the reference, which has no measurement code.) */
+typedef struct {
+    double fp32_tflops;
+    double normals_per_s;
+    int32_t sm_count;
+} rg_peaks;
+int rg_probe_peaks(rg_peaks *out, void *stream);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* RISKGPU_H */
