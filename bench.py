@@ -55,7 +55,7 @@ NCU_TRAFFIC_BYTES = None
 def parse():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--steps", type=int, default=30)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="riskgpu", choices=["riskgpu", "reference"])
     ap.add_argument("--paths", type=int, default=100_000_000)
@@ -308,7 +308,7 @@ def engine_arm(args):
     achieved = flops_per_path * args.paths / (ms_per_step * 1e-3) / 1e12
     t_ideal = (flops_per_path / (peaks["fp32_tflops"] * 1e12)
                + normals_per_path / peaks["normals_per_s"]) * args.paths
-    roofline = {"bound": "alu", "kernel": "mc_plain_small_kernel<64,philox>",
+    roofline = {"bound": "alu", "kernel": "rg::mc_rows_kernel<13,true> (N=50)",
                 "achieved": achieved, "peak": peaks["fp32_tflops"], "unit": "TFLOP/s",
                 "frac": achieved / peaks["fp32_tflops"],
                 "peak_source": "measured live: FP32 FMA micro-kernel (rg_probe_peaks)",

@@ -151,6 +151,21 @@ static int validate_query(const Portfolio *p, const rg_query *q)
     return RG_OK;
 }
 
+// The counting kernel for a query: the outer-product kernel with the factor
+// in parameter space for the Philox layout (RG_PLAIN_KERNEL=smem selects the
+// row-order shared-memory kernel instead, for comparisons), the row-order
+// kernel for the reference's XORWOW layout.
+static cudaError_t launch_counting(const Portfolio *p, const rg_query *q, const PlainArgs &a,
+                                   int sm_count, cudaStream_t s)
+{
+    if (q->rng == RG_RNG_PHILOX && p->n <= fused_max_n() && !env_contains("RG_PLAIN_KERNEL", "smem")) {
+        float hmu[64];
+        for (int i = 0; i < p->n; i++) hmu[i] = (float)((double)q->horizon * p->h_mu[(size_t)i]);
+        return launch_fused(a, p->h_Lp.data(), hmu, p->h_w.data(), sm_count, s);
+    }
+    return launch_plain_small(a, q->rng, sm_count, s);
+}
+
 static PlainArgs make_args(const Portfolio *p, const rg_query *q, unsigned long long *d_counts)
 {
     PlainArgs a;
@@ -309,6 +324,12 @@ int rg_portfolio_create(int32_t n, const double *mu, const double *sigma, int64_
     }
     p->wsw = aux[0];
     p->wmu = aux[1];
+    p->h_Lp.resize((size_t)packed_len(n));
+    p->h_mu.resize((size_t)n);
+    p->h_w.resize((size_t)n);
+    RG_CUDA_TRY(cudaMemcpy(p->h_Lp.data(), p->d_Lp, p->h_Lp.size() * sizeof(float), cudaMemcpyDeviceToHost));
+    RG_CUDA_TRY(cudaMemcpy(p->h_mu.data(), p->d_mu64, (size_t)n * sizeof(double), cudaMemcpyDeviceToHost));
+    RG_CUDA_TRY(cudaMemcpy(p->h_w.data(), p->d_w32, (size_t)n * sizeof(float), cudaMemcpyDeviceToHost));
     cudaFree(dA);
     cudaFree(dW);
     cudaEventDestroy(e0);
@@ -366,7 +387,7 @@ int rg_launch_counts(const rg_portfolio *h, const rg_query *q, unsigned long lon
     if (st) return st;
     cudaStream_t s = stream ? (cudaStream_t)stream : ctx->stream;
     cudaError_t e = cudaMemsetAsync(d_counts, 0, 2 * sizeof(unsigned long long), s);
-    if (e == cudaSuccess) e = launch_plain_small(make_args(p, q, d_counts), q->rng, ctx->sm_count, s);
+    if (e == cudaSuccess) e = launch_counting(p, q, make_args(p, q, d_counts), ctx->sm_count, s);
     if (e != cudaSuccess) return set_error(RG_ERR_CUDA, "launch failed: %s", cudaGetErrorString(e));
     return RG_OK;
 }
@@ -392,7 +413,7 @@ int rg_simulate(const rg_portfolio *h, const rg_query *q, rg_result *out, void *
     RG_CUDA_TRY(cudaEventCreate(&e0));
     RG_CUDA_TRY(cudaEventCreate(&e1));
     RG_CUDA_TRY(cudaEventRecord(e0, s));
-    RG_CUDA_TRY(launch_plain_small(make_args(p, q, d_counts), q->rng, ctx->sm_count, s));
+    RG_CUDA_TRY(launch_counting(p, q, make_args(p, q, d_counts), ctx->sm_count, s));
     RG_CUDA_TRY(cudaEventRecord(e1, s));
     RG_CUDA_TRY(cudaMemcpyAsync(counts, d_counts, sizeof(counts), cudaMemcpyDeviceToHost, s));
     RG_CUDA_TRY(cudaFreeAsync(d_counts, s));

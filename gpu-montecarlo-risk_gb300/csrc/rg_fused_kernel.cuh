@@ -1,0 +1,162 @@
+// Plain fused FP32 Monte Carlo kernel, engine (Philox) layout, N <= 64.
+//
+// Same computation as the reference kernel monte_carlo_kernel
+// (src/05-GPU/monte_carlos_cuda.cu:23-72), organised for issue throughput on
+// sm_103a:
+//
+//  * One thread owns one path at a time (grid-stride over paths, grid =
+//    SMs x resident CTAs).  Nothing per path reaches HBM unless the caller
+//    asks for S or w.R per path.
+//  * Row order with packed FP32 pairs.  Row group g (rows 4g..4g+3) needs
+//    the normals of quads 0..g; the normals of quad g+1 (one Philox4x32-10
+//    block per day, Box-Muller, summed over the H days) are drawn while group
+//    g is accumulated, so generator latency hides behind FMAs, and they are
+//    kept as float2 pairs.  Each row accumulates (L[i][j], L[i][j+1]) x
+//    (z_j, z_j+1) into a float2 with __ffma2_rn (two FMAs per instruction,
+//    sm_100+), four rows giving four independent chains; the row value is
+//    H mu_i + sum.x + sum.y.  Rows of group g are final at once: compared
+//    with -x and folded into S and w.R.
+//  * L (packed lower rows), H*mu and w live in the kernel's parameter space,
+//    indexed with compile-time offsets, so every FMA takes its L pair as a
+//    constant-bank operand: no shared-memory or global loads in the loop.
+//    The parameter block is at most 64 packed rows (8.7 KB) plus 2 x 256 B.
+//  * Counts: per-thread integers -> warp reduction -> one 64-bit atomic per
+//    CTA per counter.
+#pragma once
+#include <cstring>
+#include "rg_internal.cuh"
+
+namespace rg {
+
+static constexpr int kFusedThreads = 256;
+
+template <int NQ>
+struct ConstBlock {
+    float4 L[packed_len(4 * NQ) / 4]; // packed rows, zero padded
+    float4 hmu[NQ];                   // H * mu, FP32 (FP64 product rounded)
+    float4 w[NQ];                     // weights (zeros when none)
+};
+
+// Normals of quad q of one path, summed over the horizon.
+template <int NQ, bool ONE_DAY>
+__device__ __forceinline__ float4 fused_quad_normals(int q, int horizon, uint32_t plo, uint32_t phi,
+                                                     const PhiloxKeys &keys)
+{
+    float4 z;
+    {
+        const uint4 w = rg_philox(make_uint4((uint32_t)q, 0u, plo, phi), keys);
+        rg_box_muller(w.x, w.y, z.x, z.y);
+        rg_box_muller(w.z, w.w, z.z, z.w);
+    }
+    if (!ONE_DAY) {
+        for (int d = 1; d < horizon; d++) {
+            const uint4 w = rg_philox(make_uint4((uint32_t)(d * NQ + q), 0u, plo, phi), keys);
+            float z0, z1, z2, z3;
+            rg_box_muller(w.x, w.y, z0, z1);
+            rg_box_muller(w.z, w.w, z2, z3);
+            z.x += z0;
+            z.y += z1;
+            z.z += z2;
+            z.w += z3;
+        }
+    }
+    return z;
+}
+
+// NQ = ceil(N/4) exactly (the launcher dispatches on it), so every row
+// group exists; rows >= N occur only in the last group, hold zeros and are
+// masked out of S.  ONE_DAY drops the horizon loop for H = 1.  Four CTAs of
+// 256 threads per SM (64 registers a thread).
+template <int NQ, bool ONE_DAY>
+__global__ void __launch_bounds__(kFusedThreads, 4) mc_rows_kernel(const PlainArgs a, const ConstBlock<NQ> cb)
+{
+    __shared__ unsigned long long sacc[2];
+    const int tid = threadIdx.x;
+    if (tid < 2) sacc[tid] = 0ull;
+    __syncthreads();
+
+    const int n = a.n;
+    int crash = 0, breach = 0;
+    const long long stride = (long long)gridDim.x * blockDim.x;
+    for (long long p = (long long)blockIdx.x * blockDim.x + tid; p < a.n_paths; p += stride) {
+        const unsigned long long path = a.path0 + (unsigned long long)p;
+        const uint32_t plo = (uint32_t)path, phi = (uint32_t)(path >> 32);
+        float2 z2[2 * NQ];
+        {
+            const float4 z = fused_quad_normals<NQ, ONE_DAY>(0, a.horizon, plo, phi, a.keys);
+            z2[0] = make_float2(z.x, z.y);
+            z2[1] = make_float2(z.z, z.w);
+        }
+        int S = 0;
+        float port = 0.f;
+#pragma unroll
+        for (int g = 0; g < NQ; g++) {
+            if (g + 1 < NQ) {
+                const float4 z = fused_quad_normals<NQ, ONE_DAY>(g + 1, a.horizon, plo, phi, a.keys);
+                z2[2 * g + 2] = make_float2(z.x, z.y);
+                z2[2 * g + 3] = make_float2(z.z, z.w);
+            }
+            float2 acc[4];
+#pragma unroll
+            for (int e = 0; e < 4; e++) acc[e] = make_float2(0.f, 0.f);
+#pragma unroll
+            for (int q = 0; q <= g; q++) {
+#pragma unroll
+                for (int e = 0; e < 4; e++) {
+                    const float4 l = cb.L[packed_row_offset(4 * g + e) / 4 + q];
+                    acc[e] = __ffma2_rn(make_float2(l.x, l.y), z2[2 * q], acc[e]);
+                    acc[e] = __ffma2_rn(make_float2(l.z, l.w), z2[2 * q + 1], acc[e]);
+                }
+            }
+#pragma unroll
+            for (int e = 0; e < 4; e++) {
+                const int i = 4 * g + e;
+                const float r = (&cb.hmu[g].x)[e] + (acc[e].x + acc[e].y);
+                const bool hit = (r < a.neg_x) && (g < NQ - 1 || i < n);
+                S += hit ? 1 : 0;
+                port = fmaf((&cb.w[g].x)[e], r, port);
+            }
+        }
+        crash += (S >= a.k) ? 1 : 0;
+        breach += (a.has_w && port < a.port_thr) ? 1 : 0;
+        if (a.s_values) a.s_values[p] = S;
+        if (a.port_values) a.port_values[p] = port;
+    }
+
+    crash = __reduce_add_sync(0xffffffffu, crash);
+    breach = __reduce_add_sync(0xffffffffu, breach);
+    if ((tid & 31) == 0) {
+        atomicAdd(&sacc[0], (unsigned long long)crash);
+        atomicAdd(&sacc[1], (unsigned long long)breach);
+    }
+    __syncthreads();
+    if (tid == 0) {
+        if (sacc[0]) atomicAdd(&a.counts[0], sacc[0]);
+        if (sacc[1]) atomicAdd(&a.counts[1], sacc[1]);
+    }
+}
+
+template <int NQ>
+static cudaError_t launch_fused_nq(const PlainArgs &a, const float *Lp_host, const float *hmu,
+                                   const float *w, int sm_count, cudaStream_t s)
+{
+    if (a.n <= 4 * (NQ - 1) || a.n > 4 * NQ) return cudaErrorInvalidValue;
+    ConstBlock<NQ> cb;
+    memset(&cb, 0, sizeof(cb));
+    memcpy(cb.L, Lp_host, sizeof(float) * (size_t)packed_len(a.n));
+    memcpy(cb.hmu, hmu, sizeof(float) * (size_t)a.n);
+    memcpy(cb.w, w, sizeof(float) * (size_t)a.n);
+    auto kern = (a.horizon == 1) ? mc_rows_kernel<NQ, true> : mc_rows_kernel<NQ, false>;
+    int per_sm = 0;
+    cudaError_t e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, kFusedThreads, 0);
+    if (e != cudaSuccess) return e;
+    if (per_sm < 1) per_sm = 1;
+    long long want = (a.n_paths + kFusedThreads - 1) / kFusedThreads;
+    long long grid = (long long)sm_count * per_sm;
+    if (want < grid) grid = want;
+    if (grid < 1) grid = 1;
+    kern<<<(unsigned)grid, kFusedThreads, 0, s>>>(a, cb);
+    return cudaGetLastError();
+}
+
+} // namespace rg

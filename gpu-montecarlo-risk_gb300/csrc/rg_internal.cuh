@@ -5,13 +5,18 @@
 //                   32x32->64 multiplies with the published multipliers and
 //                   Weyl key increments.  Round keys are precomputed on the
 //                   host (they depend only on the seed).
-//   rg_box_muller   Box-Muller (Box & Muller 1958) on two 32-bit words:
-//                   u = w 2^-32 + 2^-33 in (0, 1], r = sqrt(-2 ln u_a),
-//                   t = 2 pi (u_b - 1/2), (z0, z1) = (r cos t, r sin t), using
-//                   the hardware approximate lg2/sqrt/sin/cos (PTX *.approx).
+//   rg_box_muller   Box-Muller (Box & Muller 1958) on two 32-bit words.
+//                   The top 23 bits of a word w form f = 1 + (w >> 9) 2^-23 in
+//                   [1, 2) by setting the exponent bits (no int->float
+//                   conversion); u_a = 2 - f in (0, 1], v = f_b - 3/2 in
+//                   [-1/2, 1/2); r = sqrt(-2 ln u_a), t = 2 pi v,
+//                   (z0, z1) = (r cos t, r sin t), using the hardware
+//                   approximate lg2/sqrt/sin/cos (PTX *.approx).  The
+//                   smallest u_a is 2^-23, so |z| <= sqrt(46 ln 2) = 5.65.
 #pragma once
 
 #include <cstdint>
+#include <vector>
 #include <cuda_runtime.h>
 
 #include "riskgpu.h"
@@ -75,18 +80,19 @@ __device__ __forceinline__ float rg_cos_approx(float x)
     return y;
 }
 
-__device__ __forceinline__ float rg_uniform(uint32_t w)
+// 1 + (w >> 9) 2^-23, exactly, in [1, 2)
+__device__ __forceinline__ float rg_one_to_two(uint32_t w)
 {
-    return __fmaf_rn(__uint2float_rn(w), 0x1p-32f, 0x1p-33f);
+    return __uint_as_float(0x3f800000u | (w >> 9));
 }
 
 __device__ __forceinline__ void rg_box_muller(uint32_t a, uint32_t b, float &z0, float &z1)
 {
-    const float ua = rg_uniform(a);
-    const float ub = rg_uniform(b);
+    const float ua = 2.0f - rg_one_to_two(a);          // (0, 1]
+    const float v = rg_one_to_two(b) - 1.5f;           // [-1/2, 1/2)
     // -2 ln(u) = -2 ln(2) log2(u)
     const float r = rg_sqrt_approx(-1.3862943611198906f * rg_lg2_approx(ua));
-    const float t = 6.283185307179586f * (ub - 0.5f);
+    const float t = 6.283185307179586f * v;
     z0 = r * rg_cos_approx(t);
     z1 = r * rg_sin_approx(t);
 }
@@ -113,6 +119,10 @@ struct Portfolio {
     int *d_info = nullptr;
     double wsw = 0.0, wmu = 0.0;
     float ms_chol = 0.f;
+    // host copies for kernels that take the factor by value
+    std::vector<float> h_Lp;   // packed rows, FP32
+    std::vector<double> h_mu;  // daily means, FP64
+    std::vector<float> h_w;    // weights, FP32 (zeros when none)
 };
 
 // Arguments of the fused counting kernels.
@@ -135,9 +145,15 @@ struct PlainArgs {
     unsigned long long *counts; // [2]
 };
 
-// Launchers (rg_mc_plain.cu).  Return cudaSuccess or the launch error.
+// Launchers.  Return cudaSuccess or the launch error.
+// rg_mc_plain.cu / rg_mc_xorwow.cu: row-order kernel, L staged in shared
+// memory; both normal layouts.
 cudaError_t launch_plain_small(const PlainArgs &a, int rng, int sm_count, cudaStream_t s);
 int plain_small_max_n();
+// rg_mc_fused.cu: outer-product kernel, L in parameter space; Philox only.
+cudaError_t launch_fused(const PlainArgs &a, const float *Lp_host, const float *hmu, const float *w,
+                         int sm_count, cudaStream_t s);
+int fused_max_n();
 
 // Cholesky (rg_cholesky.cu): factor, pack and portfolio moments.
 cudaError_t launch_cholesky(const double *A, long long lda, int n, const double *w,

@@ -218,19 +218,19 @@ void orc_philox4x32_10(const uint32_t ctr_in[4], const uint32_t key_in[2], uint3
     out[0] = c0; out[1] = c1; out[2] = c2; out[3] = c3;
 }
 
-/* Uniform in (0,1] built exactly as the engine builds it in FP32:
- * u = fmaf((float)w, 2^-32, 2^-33). */
-static inline float engine_uniform(uint32_t w) { return fmaf((float)w, 0x1p-32f, 0x1p-33f); }
+/* The engine's 23-bit fraction of a word: f = 1 + (w >> 9) 2^-23 in [1, 2)
+ * (exact in FP32 and FP64). */
+static inline double engine_one_to_two(uint32_t w) { return 1.0 + (double)(w >> 9) * 0x1p-23; }
 
-/* Box-Muller on one pair of 32-bit words, in FP64 from the engine's FP32
- * uniforms: z0 = r cos(t), z1 = r sin(t), r = sqrt(-2 ln u_a),
- * t = 2 pi (u_b - 1/2). */
+/* Box-Muller on one pair of 32-bit words, in FP64 from the engine's
+ * uniforms u_a = 2 - f(a) in (0, 1], v = f(b) - 3/2 in [-1/2, 1/2):
+ * z0 = r cos(t), z1 = r sin(t), r = sqrt(-2 ln u_a), t = 2 pi v. */
 static inline void box_muller(uint32_t a, uint32_t b, double *z0, double *z1)
 {
     const double two_pi = 6.283185307179586476925286766559;
-    double ua = (double)engine_uniform(a), ub = (double)engine_uniform(b);
+    double ua = 2.0 - engine_one_to_two(a), v = engine_one_to_two(b) - 1.5;
     double r = sqrt(-2.0 * log(ua));
-    double t = two_pi * (ub - 0.5);
+    double t = two_pi * v;
     *z0 = r * cos(t);
     *z1 = r * sin(t);
 }
