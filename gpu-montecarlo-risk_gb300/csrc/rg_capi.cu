@@ -12,6 +12,7 @@
 // Process-global state: one context per CUDA device (stream, timing events,
 // SM count), created on first use; everything else is owned by the handles.
 #include <cmath>
+#include <algorithm>
 #include <climits>
 #include <cstdarg>
 #include <cstdio>
@@ -148,22 +149,72 @@ static int validate_query(const Portfolio *p, const rg_query *q)
     if (p && p->n > plain_small_max_n())
         return set_error(RG_ERR_UNSUPPORTED, "N = %d exceeds this kernel's limit %d", p->n,
                          plain_small_max_n());
+    if (q->var_level > 0.0) {
+        if (p && !p->has_w) return set_error(RG_ERR_INVALID, "VaR/CVaR need portfolio weights");
+        if (q->rng != RG_RNG_PHILOX)
+            return set_error(RG_ERR_UNSUPPORTED, "VaR/CVaR are computed in the Philox layout only");
+    }
     return RG_OK;
 }
 
-// The counting kernel for a query: the outer-product kernel with the factor
-// in parameter space for the Philox layout (RG_PLAIN_KERNEL=smem selects the
-// row-order shared-memory kernel instead, for comparisons), the row-order
-// kernel for the reference's XORWOW layout.
+// Inverse standard normal CDF by bisection on erfc (only used to place the
+// VaR band; 200 halvings reach double precision).
+static double inv_norm_cdf(double prob)
+{
+    double lo = -40.0, hi = 40.0;
+    for (int it = 0; it < 200; it++) {
+        const double mid = 0.5 * (lo + hi);
+        if (0.5 * std::erfc(-mid / std::sqrt(2.0)) < prob) lo = mid; else hi = mid;
+    }
+    return 0.5 * (lo + hi);
+}
+
+// The counting kernel for a query: the fused kernel with the factor in
+// parameter space for the Philox layout (RG_PLAIN_KERNEL=smem selects the
+// shared-memory row kernel instead, for comparisons; VaR passes always use
+// the fused kernel), the shared-memory row kernel for the reference's XORWOW
+// layout.
 static cudaError_t launch_counting(const Portfolio *p, const rg_query *q, const PlainArgs &a,
                                    int sm_count, cudaStream_t s)
 {
-    if (q->rng == RG_RNG_PHILOX && p->n <= fused_max_n() && !env_contains("RG_PLAIN_KERNEL", "smem")) {
+    if (q->rng == RG_RNG_PHILOX && p->n <= fused_max_n() &&
+        (a.var_mode != 0 || !env_contains("RG_PLAIN_KERNEL", "smem"))) {
         float hmu[64];
         for (int i = 0; i < p->n; i++) hmu[i] = (float)((double)q->horizon * p->h_mu[(size_t)i]);
         return launch_fused(a, p->h_Lp.data(), hmu, p->h_w.data(), sm_count, s);
     }
     return launch_plain_small(a, q->rng, sm_count, s);
+}
+
+// Device scratch of one query: counters, VaR tail sums, candidate count,
+// histogram and candidate list, carved from one stream-ordered allocation.
+struct QueryScratch {
+    unsigned long long *counts = nullptr;  // [2]
+    unsigned long long *counts2 = nullptr; // [2] counters of the extra VaR passes (discarded)
+    unsigned long long *tail = nullptr;    // [2]
+    unsigned int *cand_count = nullptr;    // [1]
+    unsigned long long *hist = nullptr;    // [kVarHistBins + 2]
+    float *cand = nullptr;                 // [cap]
+    unsigned int cap = 0;
+    void *base = nullptr;
+};
+
+static cudaError_t scratch_alloc(QueryScratch &sc, unsigned int cap, bool with_var, cudaStream_t s)
+{
+    const size_t head = 8 * 2 + 8 * 2 + 8 * 2 + 8;
+    const size_t hist = with_var ? 8 * (size_t)(kVarHistBins + 2) : 0;
+    const size_t total = head + hist + 4 * (size_t)(with_var ? cap : 0) + 16;
+    cudaError_t e = cudaMallocAsync(&sc.base, total, s);
+    if (e != cudaSuccess) return e;
+    char *b = (char *)sc.base;
+    sc.counts = (unsigned long long *)b;
+    sc.counts2 = sc.counts + 2;
+    sc.tail = sc.counts + 4;
+    sc.cand_count = (unsigned int *)(sc.counts + 6);
+    sc.hist = with_var ? (unsigned long long *)(b + head) : nullptr;
+    sc.cand = with_var ? (float *)(b + head + hist) : nullptr;
+    sc.cap = with_var ? cap : 0;
+    return cudaMemsetAsync(sc.base, 0, head, s);
 }
 
 static PlainArgs make_args(const Portfolio *p, const rg_query *q, unsigned long long *d_counts)
@@ -402,42 +453,165 @@ int rg_simulate(const rg_portfolio *h, const rg_query *q, rg_result *out, void *
     st = get_ctx(&ctx, nullptr);
     if (st) return st;
     cudaStream_t s = stream ? (cudaStream_t)stream : ctx->stream;
-    unsigned long long *d_counts = nullptr;
-    unsigned long long counts[2] = {0, 0};
+    const bool want_var = q->var_level > 0.0;
+    const int64_t M = q->n_paths;
+    const int64_t T = want_var ? rg_tail_count(M, q->var_level) : 0;
+
+    // predicted band of the (1-level) quantile of w.R: the H-day portfolio
+    // return is N(H w.mu, H w'Sigma w); half-width 10 standard errors of the
+    // sample quantile plus 1e-3 sd
+    double band_lo = 0.0, band_hi = 0.0, sd = 0.0, mean = 0.0;
+    unsigned int cap = 0;
+    if (want_var) {
+        mean = (double)q->horizon * p->wmu;
+        sd = std::sqrt((double)q->horizon * p->wsw);
+        const double alpha = q->var_level;
+        const double z = inv_norm_cdf(1.0 - alpha);
+        const double dens = std::exp(-0.5 * z * z) / std::sqrt(2.0 * M_PI) / sd;
+        const double se = std::sqrt(alpha * (1.0 - alpha) / (double)M) / dens;
+        const double half = 10.0 * se + 1e-3 * sd;
+        // RG_FAULT_INJECT=varband displaces the band by 5 sd (host-side
+        // injection that exercises the histogram fallback)
+        const double shift = env_contains("RG_FAULT_INJECT", "varband") ? 5.0 * sd : 0.0;
+        band_lo = mean + sd * z - half + shift;
+        band_hi = mean + sd * z + half + shift;
+        const double expect = (double)M * dens * 2.0 * half;
+        cap = (unsigned int)std::min(4.0 * expect + 4096.0, 64.0 * 1024 * 1024);
+    }
+    QueryScratch sc;
     cudaEvent_t e0 = nullptr, e1 = nullptr;
-    float ms = 0.f;
-    st = admit(64);
+    float ms = 0.f, ms_pass = 0.f;
+    unsigned long long counts[2] = {0, 0}, tail[2] = {0, 0};
+    unsigned int ncand = 0;
+    std::vector<float> cand;
+    std::vector<unsigned long long> hist;
+    int passes = 0;
+    int64_t n_tail = 0;
+    PlainArgs a;
+    st = admit(64 + (size_t)cap * 4 + 8 * (kVarHistBins + 2));
     if (st) return st;
-    RG_CUDA_TRY(cudaMallocAsync((void **)&d_counts, 2 * sizeof(unsigned long long), s));
-    RG_CUDA_TRY(cudaMemsetAsync(d_counts, 0, 2 * sizeof(unsigned long long), s));
+    RG_CUDA_TRY(scratch_alloc(sc, cap, want_var, s));
     RG_CUDA_TRY(cudaEventCreate(&e0));
     RG_CUDA_TRY(cudaEventCreate(&e1));
+    a = make_args(p, q, sc.counts);
+    if (want_var) {
+        a.var_mode = 1;
+        a.sel_bins = 1;
+        a.sel_target = 0;
+        a.sel_lo = (float)band_lo;
+        a.sel_inv_w = (float)(1.0 / (band_hi - band_lo));
+        a.cand = sc.cand;
+        a.cand_count = sc.cand_count;
+        a.cand_cap = sc.cap;
+        a.tail = sc.tail;
+        a.hist = sc.hist;
+    }
     RG_CUDA_TRY(cudaEventRecord(e0, s));
-    RG_CUDA_TRY(launch_counting(p, q, make_args(p, q, d_counts), ctx->sm_count, s));
+    RG_CUDA_TRY(launch_counting(p, q, a, ctx->sm_count, s));
     RG_CUDA_TRY(cudaEventRecord(e1, s));
-    RG_CUDA_TRY(cudaMemcpyAsync(counts, d_counts, sizeof(counts), cudaMemcpyDeviceToHost, s));
-    RG_CUDA_TRY(cudaFreeAsync(d_counts, s));
-    d_counts = nullptr;
+    RG_CUDA_TRY(cudaMemcpyAsync(counts, sc.counts, sizeof(counts), cudaMemcpyDeviceToHost, s));
+    if (want_var) {
+        RG_CUDA_TRY(cudaMemcpyAsync(tail, sc.tail, sizeof(tail), cudaMemcpyDeviceToHost, s));
+        RG_CUDA_TRY(cudaMemcpyAsync(&ncand, sc.cand_count, sizeof(ncand), cudaMemcpyDeviceToHost, s));
+    }
     RG_CUDA_TRY(cudaStreamSynchronize(s));
     cudaEventElapsedTime(&ms, e0, e1);
+    passes = 1;
+    n_tail = (int64_t)tail[0];
+    if (want_var && !(n_tail < T && T <= n_tail + (int64_t)ncand && ncand <= sc.cap)) {
+        // The band missed the order statistic: histogram pass over
+        // mean -+ 12 sd, then a select pass on the bin that holds it.
+        hist.assign(kVarHistBins + 2, 0ull);
+        a.counts = sc.counts2;
+        a.var_mode = 2;
+        a.sel_bins = kVarHistBins;
+        a.sel_lo = (float)(mean - 12.0 * sd);
+        a.sel_inv_w = (float)(kVarHistBins / (24.0 * sd));
+        RG_CUDA_TRY(cudaMemsetAsync(sc.hist, 0, hist.size() * 8, s));
+        RG_CUDA_TRY(cudaEventRecord(e0, s));
+        RG_CUDA_TRY(launch_counting(p, q, a, ctx->sm_count, s));
+        RG_CUDA_TRY(cudaEventRecord(e1, s));
+        RG_CUDA_TRY(cudaMemcpyAsync(hist.data(), sc.hist, hist.size() * 8, cudaMemcpyDeviceToHost, s));
+        RG_CUDA_TRY(cudaStreamSynchronize(s));
+        cudaEventElapsedTime(&ms_pass, e0, e1);
+        ms += ms_pass;
+        int64_t cum = 0;
+        int j = 0;
+        for (; j < (int)hist.size(); j++) {
+            if (cum + (int64_t)hist[(size_t)j] >= T) break;
+            cum += (int64_t)hist[(size_t)j];
+        }
+        if (j >= (int)hist.size()) {
+            st = set_error(RG_ERR_CUDA, "VaR histogram holds fewer than %lld paths", (long long)T);
+            goto fail;
+        }
+        const unsigned int need = (unsigned int)hist[(size_t)j];
+        if (need > sc.cap) {
+            RG_CUDA_TRY(cudaFreeAsync(sc.base, s));
+            sc.base = nullptr;
+            RG_CUDA_TRY(scratch_alloc(sc, need, true, s));
+            a.counts = sc.counts2;
+            a.cand = sc.cand;
+            a.cand_count = sc.cand_count;
+            a.tail = sc.tail;
+            a.hist = sc.hist;
+        }
+        a.var_mode = 1;
+        a.sel_target = j - 1;
+        a.cand_cap = sc.cap;
+        RG_CUDA_TRY(cudaMemsetAsync(sc.tail, 0, 2 * 8, s));
+        RG_CUDA_TRY(cudaMemsetAsync(sc.cand_count, 0, 4, s));
+        RG_CUDA_TRY(cudaEventRecord(e0, s));
+        RG_CUDA_TRY(launch_counting(p, q, a, ctx->sm_count, s));
+        RG_CUDA_TRY(cudaEventRecord(e1, s));
+        RG_CUDA_TRY(cudaMemcpyAsync(tail, sc.tail, sizeof(tail), cudaMemcpyDeviceToHost, s));
+        RG_CUDA_TRY(cudaMemcpyAsync(&ncand, sc.cand_count, sizeof(ncand), cudaMemcpyDeviceToHost, s));
+        RG_CUDA_TRY(cudaStreamSynchronize(s));
+        cudaEventElapsedTime(&ms_pass, e0, e1);
+        ms += ms_pass;
+        passes = 3;
+        n_tail = (int64_t)tail[0];
+        if (n_tail != cum || ncand != need || ncand > sc.cap) {
+            st = set_error(RG_ERR_CUDA, "VaR select pass disagrees with its histogram");
+            goto fail;
+        }
+    }
+    if (want_var) {
+        cand.resize(ncand);
+        if (ncand)
+            RG_CUDA_TRY(cudaMemcpyAsync(cand.data(), sc.cand, (size_t)ncand * 4, cudaMemcpyDeviceToHost, s));
+        RG_CUDA_TRY(cudaStreamSynchronize(s));
+    }
+    RG_CUDA_TRY(cudaFreeAsync(sc.base, s));
+    sc.base = nullptr;
     memset(out, 0, sizeof(*out));
-    out->n_paths = q->n_paths;
+    out->n_paths = M;
     out->crash_count = (int64_t)counts[0];
     out->breach_count = (int64_t)counts[1];
-    rg_estimator_stats(out->crash_count, q->n_paths, &out->p_crash, &out->se_crash, &out->ci_lower,
-                       &out->ci_upper);
-    rg_estimator_stats(out->breach_count, q->n_paths, &out->p_breach, &out->se_breach, nullptr, nullptr);
+    rg_estimator_stats(out->crash_count, M, &out->p_crash, &out->se_crash, &out->ci_lower, &out->ci_upper);
+    rg_estimator_stats(out->breach_count, M, &out->p_breach, &out->se_breach, nullptr, nullptr);
     out->var = NAN;
     out->cvar = NAN;
-    out->tail_count = 0;
-    out->var_passes = 0;
+    if (want_var) {
+        // the T-th smallest w.R overall is the (T - n_tail)-th smallest candidate
+        const size_t kth = (size_t)(T - n_tail - 1);
+        std::nth_element(cand.begin(), cand.begin() + (long)kth, cand.end());
+        const float vport = cand[kth];
+        double tail_sum = (double)(long long)tail[1] * 0x1p-32;
+        for (size_t i = 0; i < kth; i++) tail_sum += -(double)cand[i];
+        tail_sum += -(double)vport;
+        out->var = -(double)vport;
+        out->cvar = tail_sum / (double)T;
+        out->tail_count = T;
+        out->var_passes = passes;
+    }
     out->ms_device = ms;
     cudaEventDestroy(e0);
     cudaEventDestroy(e1);
     return RG_OK;
 fail:
     cudaStreamSynchronize(s);
-    if (d_counts) cudaFree(d_counts);
+    if (sc.base) cudaFree(sc.base);
     if (e0) cudaEventDestroy(e0);
     if (e1) cudaEventDestroy(e1);
     return st;

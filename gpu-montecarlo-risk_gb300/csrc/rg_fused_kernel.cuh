@@ -63,17 +63,88 @@ __device__ __forceinline__ float4 fused_quad_normals(int q, int horizon, uint32_
     return z;
 }
 
+// VaR bookkeeping of one path (see PlainArgs): histogram or select pass.
+__device__ __forceinline__ void var_path(const PlainArgs &a, float port, unsigned int *shist,
+                                         int &n_tail, long long &tail_fx)
+{
+    const float t = (port - a.sel_lo) * a.sel_inv_w;
+    const int b = (t < 0.f) ? -1 : (t >= (float)a.sel_bins ? a.sel_bins : (int)t);
+    if (a.var_mode == 2) {
+        atomicAdd(&shist[b + 1], 1u);
+        return;
+    }
+    if (b < a.sel_target) {
+        n_tail++;
+        tail_fx += __float2ll_rn(-port * 4294967296.0f);
+    }
+    // warp-aggregated append of the candidates
+    const bool cand = (b == a.sel_target);
+    const unsigned act = __activemask();
+    const unsigned m = __ballot_sync(act, cand);
+    if (m) {
+        const int lane = threadIdx.x & 31;
+        const int leader = __ffs(m) - 1;
+        unsigned base = 0;
+        if (lane == leader) base = atomicAdd(a.cand_count, (unsigned)__popc(m));
+        base = __shfl_sync(act, base, leader);
+        const unsigned idx = base + __popc(m & ((1u << lane) - 1u));
+        if (cand && idx < a.cand_cap) a.cand[idx] = port;
+    }
+}
+
+// Per-CTA reduction of the counters: warp sums, one 64-bit atomic per CTA
+// per counter, and the CTA's histogram merged into the global one.
+__device__ __forceinline__ void cta_flush(const PlainArgs &a, int crash, int breach, int n_tail,
+                                          long long tail_fx, unsigned long long *sacc,
+                                          unsigned int *shist)
+{
+    const int tid = threadIdx.x;
+    crash = __reduce_add_sync(0xffffffffu, crash);
+    breach = __reduce_add_sync(0xffffffffu, breach);
+    if (shist) {
+        n_tail = __reduce_add_sync(0xffffffffu, n_tail);
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) tail_fx += __shfl_xor_sync(0xffffffffu, tail_fx, o);
+    }
+    if ((tid & 31) == 0) {
+        atomicAdd(&sacc[0], (unsigned long long)crash);
+        atomicAdd(&sacc[1], (unsigned long long)breach);
+        if (shist) {
+            atomicAdd(&sacc[2], (unsigned long long)n_tail);
+            atomicAdd(&sacc[3], (unsigned long long)tail_fx);
+        }
+    }
+    __syncthreads();
+    if (tid == 0) {
+        if (sacc[0]) atomicAdd(&a.counts[0], sacc[0]);
+        if (sacc[1]) atomicAdd(&a.counts[1], sacc[1]);
+        if (shist && a.var_mode == 1) {
+            if (sacc[2]) atomicAdd(&a.tail[0], sacc[2]);
+            if (sacc[3]) atomicAdd(&a.tail[1], sacc[3]);
+        }
+    }
+    if (shist && a.var_mode == 2)
+        for (int t = tid; t < a.sel_bins + 2; t += blockDim.x)
+            if (shist[t]) atomicAdd(&a.hist[t], (unsigned long long)shist[t]);
+}
+
 // NQ = ceil(N/4) exactly (the launcher dispatches on it), so every row
 // group exists; rows >= N occur only in the last group, hold zeros and are
 // masked out of S.  ONE_DAY drops the horizon loop for H = 1.  Four CTAs of
-// 256 threads per SM (64 registers a thread).
-template <int NQ, bool ONE_DAY>
+// 256 threads per SM (64 registers a thread).  VAR adds the VaR/CVaR
+// bookkeeping of var_path (the counting-only form carries none of it).
+template <int NQ, bool ONE_DAY, bool VAR>
 __global__ void __launch_bounds__(kFusedThreads, 4) mc_rows_kernel(const PlainArgs a, const ConstBlock<NQ> cb)
 {
-    __shared__ unsigned long long sacc[2];
+    __shared__ unsigned long long sacc[4];
+    __shared__ unsigned int shist[VAR ? kVarHistBins + 2 : 1];
     const int tid = threadIdx.x;
-    if (tid < 2) sacc[tid] = 0ull;
+    if (tid < 4) sacc[tid] = 0ull;
+    if (VAR && a.var_mode == 2)
+        for (int t = tid; t < a.sel_bins + 2; t += blockDim.x) shist[t] = 0u;
     __syncthreads();
+    int n_tail = 0;
+    long long tail_fx = 0;
 
     const int n = a.n;
     int crash = 0, breach = 0;
@@ -121,19 +192,9 @@ __global__ void __launch_bounds__(kFusedThreads, 4) mc_rows_kernel(const PlainAr
         breach += (a.has_w && port < a.port_thr) ? 1 : 0;
         if (a.s_values) a.s_values[p] = S;
         if (a.port_values) a.port_values[p] = port;
+        if (VAR) var_path(a, port, shist, n_tail, tail_fx);
     }
-
-    crash = __reduce_add_sync(0xffffffffu, crash);
-    breach = __reduce_add_sync(0xffffffffu, breach);
-    if ((tid & 31) == 0) {
-        atomicAdd(&sacc[0], (unsigned long long)crash);
-        atomicAdd(&sacc[1], (unsigned long long)breach);
-    }
-    __syncthreads();
-    if (tid == 0) {
-        if (sacc[0]) atomicAdd(&a.counts[0], sacc[0]);
-        if (sacc[1]) atomicAdd(&a.counts[1], sacc[1]);
-    }
+    cta_flush(a, crash, breach, n_tail, tail_fx, sacc, VAR ? shist : nullptr);
 }
 
 template <int NQ>
@@ -146,7 +207,8 @@ static cudaError_t launch_fused_nq(const PlainArgs &a, const float *Lp_host, con
     memcpy(cb.L, Lp_host, sizeof(float) * (size_t)packed_len(a.n));
     memcpy(cb.hmu, hmu, sizeof(float) * (size_t)a.n);
     memcpy(cb.w, w, sizeof(float) * (size_t)a.n);
-    auto kern = (a.horizon == 1) ? mc_rows_kernel<NQ, true> : mc_rows_kernel<NQ, false>;
+    auto kern = (a.var_mode != 0) ? mc_rows_kernel<NQ, false, true>
+                : (a.horizon == 1) ? mc_rows_kernel<NQ, true, false> : mc_rows_kernel<NQ, false, false>;
     int per_sm = 0;
     cudaError_t e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, kFusedThreads, 0);
     if (e != cudaSuccess) return e;

@@ -143,7 +143,26 @@ struct PlainArgs {
     int *s_values;
     float *port_values;
     unsigned long long *counts; // [2]
+    // VaR / CVaR passes (kernels instantiated with VaR support only).
+    // Every path's portfolio return w.R falls in bin
+    //   b = floor((w.R - sel_lo) * sel_inv_w), clamped to [-1, sel_bins].
+    // var_mode 1 (select): b < sel_target -> tail (count, fixed-point loss
+    //   sum); b == sel_target -> candidate appended to cand[].
+    // var_mode 2 (histogram): counts per bin into hist[sel_bins + 2].
+    int var_mode;
+    int sel_bins;
+    int sel_target;
+    float sel_lo;
+    float sel_inv_w;
+    float *cand;
+    unsigned int *cand_count;
+    unsigned int cand_cap;
+    unsigned long long *tail;   // [0] tail paths, [1] sum of -w.R * 2^32 (int64 bits)
+    unsigned long long *hist;   // [sel_bins + 2]
 };
+
+// Shared-memory histogram size of the VaR pass: bins plus under/overflow.
+static constexpr int kVarHistBins = 4096;
 
 // Launchers.  Return cudaSuccess or the launch error.
 // rg_mc_plain.cu / rg_mc_xorwow.cu: row-order kernel, L staged in shared

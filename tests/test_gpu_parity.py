@@ -256,3 +256,103 @@ def test_runner_binary_end_to_end(gpu, tmp_path):
     count = int(out.stdout.split("Extreme Events Count: ")[1].split()[0])
     direct = gpu.run(p.mu, p.sigma, None, gpu.make_query(200_000, 67, x=p.x, k=p.k))
     assert count == direct["crash_count"]
+
+
+# ------------------------------------------------------------------ VaR / CVaR
+def _var_case(gpu, n_paths, level=0.99, horizon=1, seed=11, n=50):
+    from riskgpu import synth
+    p = synth.one_factor_50(n_paths=1)
+    if n != 50:
+        rng = np.random.default_rng(n)
+        mu, sigma, _, _ = synth.one_factor_sigma(rng, n)
+        w = rng.dirichlet(np.ones(n))
+    else:
+        mu, sigma, w = p.mu, p.sigma, p.weights
+    port = gpu.Portfolio(mu, sigma, w)
+    torch = _torch()
+    W = torch.empty(n_paths, dtype=torch.float32, device="cuda")
+    q = gpu.make_query(n_paths, seed, x=0.03, k=5, horizon=horizon, port_threshold=-0.03,
+                       var_level=level, d_port_values=W.data_ptr())
+    r = port.simulate(q)
+    torch.cuda.synchronize()
+    return r, W.cpu().numpy().astype(np.float64), (mu, sigma, w)
+
+
+@pytest.mark.parametrize("M,level,horizon", [(200_000, 0.99, 1), (1_000_003, 0.975, 3), (1000, 0.99, 1),
+                                             (100, 0.99, 1), (1, 0.5, 1)])
+def test_var_cvar_exact_order_statistics(gpu, oracle, M, level, horizon):
+    """VaR/CVaR from the fused band pass equal the order statistics of the
+    engine's own per-path portfolio returns (definition of the oracle:
+    T = ceil((1-level) M) largest losses; VaR the smallest of them, CVaR their
+    mean)."""
+    r, W, _ = _var_case(gpu, M, level, horizon)
+    var, cvar, T = oracle.var_cvar(W, level)
+    assert r["tail_count"] == T
+    assert r["var"] == var
+    assert abs(r["cvar"] - cvar) <= 1e-12 + 1e-9 * abs(cvar)
+    assert r["var_passes"] == 1
+
+
+def test_var_fallback_passes(gpu, oracle, monkeypatch):
+    """With the predicted band displaced (host-side injection) the histogram
+    pass and the bin-select pass find the same order statistics."""
+    monkeypatch.setenv("RG_FAULT_INJECT", "varband")
+    r, W, _ = _var_case(gpu, 300_000, 0.99)
+    var, cvar, T = oracle.var_cvar(W, 0.99)
+    assert r["var_passes"] == 3
+    assert r["var"] == var and abs(r["cvar"] - cvar) <= 1e-9 * abs(cvar)
+
+
+def test_var_matches_fp64_oracle_per_path(gpu, oracle):
+    """Against the FP64 restatement of the same paths: VaR/CVaR within the
+    per-path return tolerance."""
+    M = 200_000
+    r, W, (mu, sigma, w) = _var_case(gpu, M, 0.99, n=20)
+    L_ref, _ = oracle.cholesky_lower(sigma)
+    ref = oracle.mc_philox(mu, L_ref, w, 1, M, 11, 0.03, 5, -0.03, want_port=True)
+    var, cvar, _ = oracle.var_cvar(ref["port"], 0.99)
+    assert abs(r["var"] - var) <= PORT_TOL and abs(r["cvar"] - cvar) <= PORT_TOL
+
+
+def test_var_cvar_vs_closed_form(gpu, oracle):
+    """2e7 paths: VaR within 3 quantile standard errors and CVaR within 3
+    of its standard error of the exact Gaussian values."""
+    from scipy.stats import norm
+    from riskgpu import synth
+    p = synth.one_factor_50(n_paths=1)
+    port = gpu.Portfolio(p.mu, p.sigma, p.weights)
+    M, a = 20_000_000, 0.99
+    r = port.simulate(gpu.make_query(M, 3, x=p.x, k=p.k, port_threshold=p.port_threshold, var_level=a))
+    cf = oracle.portfolio_closed_form(p.mu, p.sigma, p.weights, 1, p.port_threshold, a)
+    z = norm.ppf(a)
+    se_q = math.sqrt(a * (1 - a) / M) / (norm.pdf(z) / cf["sd"])
+    assert abs(r["var"] - cf["var"]) < 3 * se_q
+    # CVaR standard error: sd of the tail losses / sqrt(T)
+    tail_sd = cf["sd"] * math.sqrt(1 + z * norm.pdf(z) / (1 - a) - (norm.pdf(z) / (1 - a)) ** 2)
+    se_c = math.sqrt((tail_sd ** 2 + a * (cf["cvar"] - cf["var"]) ** 2) / ((1 - a) * M))
+    assert abs(r["cvar"] - cf["cvar"]) < 3 * se_c
+
+
+def test_var_requires_weights_and_philox(gpu):
+    from riskgpu import synth
+    p = synth.one_factor_20(n_paths=1)
+    port = gpu.Portfolio(p.mu, p.sigma)
+    with pytest.raises(gpu.RiskGpuError) as e:
+        port.simulate(gpu.make_query(1000, 1, var_level=0.99))
+    assert e.value.status == gpu.RG_ERR_INVALID
+    port = gpu.Portfolio(p.mu, p.sigma, p.weights)
+    with pytest.raises(gpu.RiskGpuError) as e:
+        port.simulate(gpu.make_query(1000, 1, var_level=0.99, rng=gpu.RNG_XORWOW_REF))
+    assert e.value.status == gpu.RG_ERR_UNSUPPORTED
+
+
+def test_var_pass_does_not_change_counts(gpu):
+    from riskgpu import synth
+    p = synth.one_factor_50(n_paths=1)
+    port = gpu.Portfolio(p.mu, p.sigma, p.weights)
+    q0 = gpu.make_query(3_000_000, 9, x=p.x, k=p.k, port_threshold=p.port_threshold)
+    q1 = gpu.make_query(3_000_000, 9, x=p.x, k=p.k, port_threshold=p.port_threshold, var_level=0.99)
+    a, b = port.simulate(q0), port.simulate(q1)
+    assert (a["crash_count"], a["breach_count"]) == (b["crash_count"], b["breach_count"])
+    c = port.simulate(q1)
+    assert (b["var"], b["cvar"]) == (c["var"], c["cvar"])
