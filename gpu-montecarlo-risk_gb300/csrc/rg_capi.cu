@@ -240,6 +240,19 @@ static PlainArgs make_args(const Portfolio *p, const rg_query *q, unsigned long 
     return a;
 }
 
+// Shared with rg_noalloc.cu (same checks, same launch selection).
+int query_check(const Portfolio *p, const rg_query *q) { return validate_query(p, q); }
+cudaError_t query_launch(const Portfolio *p, const rg_query *q, const PlainArgs &a, int sm_count,
+                         cudaStream_t s)
+{
+    return launch_counting(p, q, a, sm_count, s);
+}
+PlainArgs query_args(const Portfolio *p, const rg_query *q, unsigned long long *d_counts)
+{
+    return make_args(p, q, d_counts);
+}
+double quantile_normal(double prob) { return inv_norm_cdf(prob); }
+
 } // namespace rg
 
 using namespace rg;

@@ -37,7 +37,8 @@ EXPORTED_SYMBOLS = [
     "rg_abi_version", "rg_status_string", "rg_last_error", "rg_device_count",
     "rg_portfolio_create", "rg_portfolio_destroy", "rg_portfolio_info_get",
     "rg_portfolio_factor", "rg_simulate", "rg_launch_counts", "rg_run",
-    "rg_estimator_stats", "rg_tail_count", "rg_probe_peaks", "get_cuda_model", "cuda_simulate",
+    "rg_estimator_stats", "rg_tail_count", "rg_probe_peaks", "rg_simulate_noalloc",
+    "get_cuda_model", "cuda_simulate",
 ]
 
 
@@ -135,6 +136,8 @@ def lib():
         L.rg_portfolio_factor.argtypes = [ctypes.c_void_p, ctypes.c_void_p]
         L.rg_simulate.argtypes = [ctypes.c_void_p, ctypes.POINTER(Query), ctypes.POINTER(Result),
                                   ctypes.c_void_p]
+        L.rg_simulate_noalloc.argtypes = [ctypes.c_void_p, ctypes.POINTER(Query), ctypes.POINTER(Result),
+                                          ctypes.c_void_p]
         L.rg_launch_counts.argtypes = [ctypes.c_void_p, ctypes.POINTER(Query), ctypes.c_void_p,
                                        ctypes.c_void_p]
         L.rg_run.argtypes = [ctypes.c_int32, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int64,

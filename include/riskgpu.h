@@ -142,6 +142,26 @@ void rg_estimator_stats(int64_t count, int64_t M, double *p, double *se, double 
 /* VaR tail size used by the engine: ceil((1-level) M), clamped to [1, M]. */
 int64_t rg_tail_count(int64_t M, double level);
 
+/* ---------------- simulation without allocation ---------------- */
+/* No counterpart in the reference.  rg_simulate() with no allocation at all,
+ * for callers that cannot call cudaMalloc where they run a query: a host
+ * that accounts for every device byte itself, a latency-critical loop where
+ * an allocation could synchronise the device, a plugin inside a framework
+ * whose allocator owns the device heap.  The portfolio (created beforehand)
+ * and the query are the inputs, `out` the output; the per-query scratch
+ * (counters, VaR histogram, VaR candidates) lives in a 1 MiB device array
+ * that every GPU loading this library holds until the process exits.
+ *  - Queries whose VaR band could need more than the array's ~253k
+ *    candidate slots (about n_paths > 2.5e8 at level 0.99) are rejected with
+ *    RG_ERR_UNSUPPORTED and a message naming the limit.
+ *  - The first call on each device looks up the array's device address
+ *    (cudaGetSymbolAddress, with that device current); make that first call
+ *    before any stream capture.
+ *  - Calls share the one array: calls whose GPU work overlaps (different
+ *    streams or host threads) race on it and must be serialised.
+ *  - `stream` NULL means the default stream; ms_device is left 0. */
+int rg_simulate_noalloc(const rg_portfolio *p, const rg_query *q, rg_result *out, void *stream);
+
 /* ---------------- measurement ---------------- */
 /* Roofline denominators of the fused kernels, measured on the current
  * device with micro-kernels timed by CUDA events on `stream`: FP32 FMA
