@@ -127,6 +127,7 @@ static void portfolio_free(Portfolio *p)
     cudaFree(p->d_L64);
     cudaFree(p->d_mu64);
     cudaFree(p->d_Lp);
+    cudaFree(p->d_Lt);
     cudaFree(p->d_w32);
     cudaFree(p->d_aux);
     cudaFree(p->d_info);
@@ -146,9 +147,16 @@ static int validate_query(const Portfolio *p, const rg_query *q)
         return set_error(RG_ERR_INVALID, "unknown precision %d", q->precision);
     if (!(q->var_level >= 0.0 && q->var_level < 1.0))
         return set_error(RG_ERR_INVALID, "var_level must be in [0, 1)");
-    if (p && p->n > plain_small_max_n())
-        return set_error(RG_ERR_UNSUPPORTED, "N = %d exceeds this kernel's limit %d", p->n,
-                         plain_small_max_n());
+    if (q->draw_mode != RG_DRAWS_DAILY && q->draw_mode != RG_DRAWS_AGGREGATED)
+        return set_error(RG_ERR_INVALID, "unknown draw mode %d", q->draw_mode);
+    if (q->rng == RG_RNG_XORWOW_REF && q->draw_mode != RG_DRAWS_DAILY)
+        return set_error(RG_ERR_UNSUPPORTED, "the reference XORWOW layout has daily draws only");
+    if (p && q->rng == RG_RNG_XORWOW_REF && p->n > plain_small_max_n())
+        return set_error(RG_ERR_UNSUPPORTED, "the reference XORWOW layout is limited to N <= %d (N = %d)",
+                         plain_small_max_n(), p->n);
+    if (p && p->n > tiled_max_n())
+        return set_error(RG_ERR_UNSUPPORTED, "N = %d exceeds the simulation limit %d", p->n,
+                         tiled_max_n());
     if (q->var_level > 0.0) {
         if (p && !p->has_w) return set_error(RG_ERR_INVALID, "VaR/CVaR need portfolio weights");
         if (q->rng != RG_RNG_PHILOX)
@@ -169,14 +177,16 @@ static double inv_norm_cdf(double prob)
     return 0.5 * (lo + hi);
 }
 
-// The counting kernel for a query: the fused kernel with the factor in
-// parameter space for the Philox layout (RG_PLAIN_KERNEL=smem selects the
-// shared-memory row kernel instead, for comparisons; VaR passes always use
-// the fused kernel), the shared-memory row kernel for the reference's XORWOW
-// layout.
+// The counting kernel for a query.  Philox layout: the fused kernel with
+// the factor in parameter space for N <= 64, the tiled kernel above
+// (RG_PLAIN_KERNEL=tiled forces the tiled kernel, =smem the shared-memory
+// row kernel, for comparisons; VaR passes never use the latter).  The
+// reference's XORWOW layout: the shared-memory row kernel.
 static cudaError_t launch_counting(const Portfolio *p, const rg_query *q, const PlainArgs &a,
                                    int sm_count, cudaStream_t s)
 {
+    if (q->rng == RG_RNG_PHILOX && (p->n > fused_max_n() || env_contains("RG_PLAIN_KERNEL", "tiled")))
+        return launch_tiled(a, p->d_Lt, q->draw_mode == RG_DRAWS_AGGREGATED, sm_count, s);
     if (q->rng == RG_RNG_PHILOX && p->n <= fused_max_n() &&
         (a.var_mode != 0 || !env_contains("RG_PLAIN_KERNEL", "smem"))) {
         float hmu[64];
@@ -234,6 +244,7 @@ static PlainArgs make_args(const Portfolio *p, const rg_query *q, unsigned long 
     a.port_thr = (float)q->port_threshold;
     a.k = q->k;
     a.has_w = p->has_w;
+    a.aggregated = (q->draw_mode == RG_DRAWS_AGGREGATED) ? 1 : 0;
     a.s_values = q->d_s_values;
     a.port_values = q->d_port_values;
     a.counts = d_counts;
@@ -331,7 +342,8 @@ int rg_portfolio_create(int32_t n, const double *mu, const double *sigma, int64_
     int st = get_ctx(&ctx, &dev);
     if (st) return st;
     const size_t nn = (size_t)n * n;
-    const size_t need = nn * 8 * (dev_in ? 1 : 2) + (size_t)n * 24 + (size_t)packed_len(n) * 4 + 64;
+    const size_t need = nn * 8 * (dev_in ? 1 : 2) + (size_t)n * 24 + (size_t)packed_len(n) * 4 +
+                        (size_t)tiled_kpad(n) * tiled_npad(n) * 4 + 64;
     st = admit(need);
     if (st) return st;
 
@@ -349,6 +361,8 @@ int rg_portfolio_create(int32_t n, const double *mu, const double *sigma, int64_
     RG_CUDA_TRY(cudaMalloc(&p->d_L64, nn * sizeof(double)));
     RG_CUDA_TRY(cudaMalloc(&p->d_mu64, (size_t)n * sizeof(double)));
     RG_CUDA_TRY(cudaMalloc(&p->d_Lp, (size_t)packed_len(n) * sizeof(float)));
+    if (n <= tiled_max_n())
+        RG_CUDA_TRY(cudaMalloc(&p->d_Lt, (size_t)tiled_kpad(n) * tiled_npad(n) * sizeof(float)));
     RG_CUDA_TRY(cudaMalloc(&p->d_w32, (size_t)n * sizeof(float)));
     RG_CUDA_TRY(cudaMalloc(&p->d_aux, 2 * sizeof(double)));
     RG_CUDA_TRY(cudaMalloc(&p->d_info, sizeof(int)));
@@ -388,6 +402,7 @@ int rg_portfolio_create(int32_t n, const double *mu, const double *sigma, int64_
     }
     p->wsw = aux[0];
     p->wmu = aux[1];
+    if (p->d_Lt) RG_CUDA_TRY(launch_build_lt(p->d_L64, n, p->d_Lt, s));
     p->h_Lp.resize((size_t)packed_len(n));
     p->h_mu.resize((size_t)n);
     p->h_w.resize((size_t)n);

@@ -205,10 +205,17 @@ static cudaError_t launch_fused_nq(const PlainArgs &a, const float *Lp_host, con
     ConstBlock<NQ> cb;
     memset(&cb, 0, sizeof(cb));
     memcpy(cb.L, Lp_host, sizeof(float) * (size_t)packed_len(a.n));
+    if (a.aggregated) {
+        // one N(0,1) draw per asset: R = H mu + (sqrt(H) L) z
+        const float sh = sqrtf((float)a.horizon);
+        float *Lf = reinterpret_cast<float *>(cb.L);
+        for (int i = 0; i < packed_len(a.n); i++) Lf[i] *= sh;
+    }
     memcpy(cb.hmu, hmu, sizeof(float) * (size_t)a.n);
     memcpy(cb.w, w, sizeof(float) * (size_t)a.n);
-    auto kern = (a.var_mode != 0) ? mc_rows_kernel<NQ, false, true>
-                : (a.horizon == 1) ? mc_rows_kernel<NQ, true, false> : mc_rows_kernel<NQ, false, false>;
+    const bool one_day = (a.horizon == 1 || a.aggregated);
+    auto kern = (a.var_mode != 0) ? (one_day ? mc_rows_kernel<NQ, true, true> : mc_rows_kernel<NQ, false, true>)
+                : one_day ? mc_rows_kernel<NQ, true, false> : mc_rows_kernel<NQ, false, false>;
     int per_sm = 0;
     cudaError_t e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, kFusedThreads, 0);
     if (e != cudaSuccess) return e;

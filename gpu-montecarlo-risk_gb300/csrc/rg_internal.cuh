@@ -114,6 +114,7 @@ struct Portfolio {
     double *d_L64 = nullptr;   // n x n row-major, zero upper
     double *d_mu64 = nullptr;  // n
     float *d_Lp = nullptr;     // packed rows (packed_len(n) floats)
+    float *d_Lt = nullptr;     // L^T FP32 [tiled_kpad(n)][tiled_npad(n)], zero padded
     float *d_w32 = nullptr;    // n (zeros when no weights)
     double *d_aux = nullptr;   // [2]: w^T Sigma w, w.mu
     int *d_info = nullptr;
@@ -140,6 +141,7 @@ struct PlainArgs {
     float port_thr;
     int k;
     int has_w;
+    int aggregated;            // draw mode RG_DRAWS_AGGREGATED
     int *s_values;
     float *port_values;
     unsigned long long *counts; // [2]
@@ -169,7 +171,14 @@ static constexpr int kVarHistBins = 4096;
 // memory; both normal layouts.
 cudaError_t launch_plain_small(const PlainArgs &a, int rng, int sm_count, cudaStream_t s);
 int plain_small_max_n();
-// rg_mc_fused.cu: outer-product kernel, L in parameter space; Philox only.
+// rg_mc_tiled.cu: general-N tiled kernel (Philox layout).
+cudaError_t launch_tiled(const PlainArgs &a, const float *Lt, bool aggregated, int sm_count,
+                         cudaStream_t s);
+cudaError_t launch_build_lt(const double *L64, int n, float *Lt, cudaStream_t s);
+int tiled_max_n();
+int tiled_npad(int n);
+int tiled_kpad(int n);
+// rg_mc_fused.cu: N <= 64 kernel, L in parameter space; Philox only.
 cudaError_t launch_fused(const PlainArgs &a, const float *Lp_host, const float *hmu, const float *w,
                          int sm_count, cudaStream_t s);
 int fused_max_n();

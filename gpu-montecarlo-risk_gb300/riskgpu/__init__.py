@@ -27,6 +27,8 @@ RG_ERR_BUSY = -9
 
 RNG_PHILOX = 0
 RNG_XORWOW_REF = 1
+DRAWS_DAILY = 0
+DRAWS_AGGREGATED = 1
 PREC_FP32 = 0
 PREC_BF16X3 = 1
 PREC_AUTO = 2
@@ -54,7 +56,8 @@ class Query(ctypes.Structure):
                 ("x", ctypes.c_double), ("port_threshold", ctypes.c_double),
                 ("rng", ctypes.c_int32), ("precision", ctypes.c_int32),
                 ("var_level", ctypes.c_double), ("d_s_values", ctypes.c_void_p),
-                ("d_port_values", ctypes.c_void_p)]
+                ("d_port_values", ctypes.c_void_p), ("draw_mode", ctypes.c_int32),
+                ("reserved", ctypes.c_int32)]
 
 
 class Result(ctypes.Structure):
@@ -165,10 +168,10 @@ def _host(a):
 
 def make_query(n_paths, seed, x=0.02, k=5, horizon=1, port_threshold=-0.02, rng=RNG_PHILOX,
                precision=PREC_AUTO, var_level=0.0, path_offset=0, d_s_values=None,
-               d_port_values=None) -> Query:
+               d_port_values=None, draw_mode=DRAWS_DAILY) -> Query:
     return Query(int(n_paths), int(path_offset), int(seed), int(horizon), int(k), float(x),
                  float(port_threshold), int(rng), int(precision), float(var_level),
-                 d_s_values, d_port_values)
+                 d_s_values, d_port_values, int(draw_mode), 0)
 
 
 class Portfolio:

@@ -53,6 +53,15 @@ typedef enum {
     RG_RNG_XORWOW_REF = 1
 } rg_rng_layout;
 
+/* How the H daily draws of an asset are formed. */
+typedef enum {
+    /* H daily N(0,1) draws summed per asset (the model as stated). */
+    RG_DRAWS_DAILY = 0,
+    /* One N(0,1) draw per asset scaled by sqrt(H): the same N(0, H)
+     * distribution of the sum, H times fewer normals, different draws. */
+    RG_DRAWS_AGGREGATED = 1
+} rg_draw_mode;
+
 /* Arithmetic of the correlation step R = H mu + L Zsum. */
 typedef enum {
     RG_PREC_FP32 = 0,   /* FP32 FMA cores (the plain fused kernel) */
@@ -88,6 +97,8 @@ typedef struct {
     double var_level;       /* e.g. 0.99; 0 disables VaR/CVaR */
     int32_t *d_s_values;    /* optional device output [n_paths]: S per path */
     float *d_port_values;   /* optional device output [n_paths]: w.R per path */
+    int32_t draw_mode;      /* rg_draw_mode */
+    int32_t reserved;       /* 0 */
 } rg_query;
 
 typedef struct {

@@ -260,11 +260,13 @@ void orc_philox_normals(uint64_t seed, uint64_t path, int n, int n_days, double 
 /* FP64 Monte Carlo in the engine's layout.  L row-major n x n (lower
  * triangle read), w may be NULL (no portfolio), paths are
  * path_offset .. path_offset+M-1.  Per-path outputs are nullable.
- * counts[0] = #{S >= k}, counts[1] = #{w.R < port_threshold}. */
+ * counts[0] = #{S >= k}, counts[1] = #{w.R < port_threshold}.
+ * aggregated = 1: one draw per asset scaled by sqrt(H) instead of the sum of
+ * H daily draws (the engine's RG_DRAWS_AGGREGATED). */
 void orc_mc_philox(int n, const double *mu, const double *L, const double *w, int n_days,
                    long long M, uint64_t path_offset, uint64_t seed, double x, int k,
                    double port_threshold, int *S_out, double *port_out, double *R_out,
-                   long long counts[2], int nthreads)
+                   long long counts[2], int nthreads, int aggregated)
 {
     long long crash = 0, breach = 0;
 #ifdef _OPENMP
@@ -278,11 +280,17 @@ void orc_mc_philox(int n, const double *mu, const double *L, const double *w, in
         double *zs = (double *)malloc(sizeof(double) * (size_t)n);
 #pragma omp for schedule(static)
         for (long long p = 0; p < M; p++) {
-            orc_philox_normals(seed, path_offset + (uint64_t)p, n, n_days, z);
-            for (int j = 0; j < n; j++) {
-                double s = 0.0;
-                for (int d = 0; d < n_days; d++) s += z[(size_t)d * n + j];
-                zs[j] = s;
+            if (aggregated) {
+                /* one N(0,1) draw per asset (day 0 of the layout) times sqrt(H) */
+                orc_philox_normals(seed, path_offset + (uint64_t)p, n, 1, z);
+                for (int j = 0; j < n; j++) zs[j] = sqrt((double)n_days) * z[j];
+            } else {
+                orc_philox_normals(seed, path_offset + (uint64_t)p, n, n_days, z);
+                for (int j = 0; j < n; j++) {
+                    double s = 0.0;
+                    for (int d = 0; d < n_days; d++) s += z[(size_t)d * n + j];
+                    zs[j] = s;
+                }
             }
             int S = 0;
             double port = 0.0;

@@ -77,7 +77,7 @@ def lib():
                                          ctypes.c_int, _dp]
         L.orc_mc_philox.argtypes = [ctypes.c_int, _dp, _dp, _dp, ctypes.c_int, ctypes.c_longlong,
                                     ctypes.c_uint64, ctypes.c_uint64, ctypes.c_double, ctypes.c_int,
-                                    ctypes.c_double, _ip, _dp, _dp, _i64p, ctypes.c_int]
+                                    ctypes.c_double, _ip, _dp, _dp, _i64p, ctypes.c_int, ctypes.c_int]
         L.orc_cholesky_lower.argtypes = [ctypes.c_int, _dp, ctypes.c_longlong, _dp]
         L.orc_cholesky_lower.restype = ctypes.c_int
         L.orc_stats.argtypes = [ctypes.c_longlong, ctypes.c_longlong, ctypes.POINTER(OrcResult)]
@@ -222,7 +222,7 @@ def philox_normals(seed, path, n, n_days=1):
 
 
 def mc_philox(mu, L, w, n_days, M, seed, x, k, port_threshold, path_offset=0,
-              want_S=False, want_port=False, want_R=False, nthreads=0):
+              want_S=False, want_port=False, want_R=False, nthreads=0, aggregated=False):
     """FP64 Monte Carlo in the engine's sampling layout (per-path parity)."""
     n = len(mu)
     mu, pmu = _d(mu)
@@ -238,7 +238,7 @@ def mc_philox(mu, L, w, n_days, M, seed, x, k, port_threshold, path_offset=0,
                         S.ctypes.data_as(_ip) if want_S else None,
                         port.ctypes.data_as(_dp) if want_port else None,
                         R.ctypes.data_as(_dp) if want_R else None,
-                        counts.ctypes.data_as(_i64p), nthreads)
+                        counts.ctypes.data_as(_i64p), nthreads, int(aggregated))
     return dict(crash=int(counts[0]), breach=int(counts[1]), S=S, port=port, R=R)
 
 

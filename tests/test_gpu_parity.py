@@ -356,3 +356,90 @@ def test_var_pass_does_not_change_counts(gpu):
     assert (a["crash_count"], a["breach_count"]) == (b["crash_count"], b["breach_count"])
     c = port.simulate(q1)
     assert (b["var"], b["cvar"]) == (c["var"], c["cvar"])
+
+
+# --------------------------------------------------------- general-N kernel
+def _factor_case(n, seed, factors=5):
+    from riskgpu import synth
+    rng = np.random.default_rng(seed)
+    if factors == 1:
+        mu, sigma, _, _ = synth.one_factor_sigma(rng, n)
+    else:
+        mu, sigma, _, _ = synth.factor_sigma(rng, n, factors, 0.5 * 0.01)
+    w = rng.dirichlet(np.ones(n))
+    return mu, sigma, w
+
+
+@pytest.mark.parametrize("n,horizon,M", [(65, 1, 20000), (100, 3, 8000), (129, 1, 8000),
+                                         (300, 2, 3000), (600, 10, 1024), (768, 1, 700)])
+def test_tiled_per_path_parity(gpu, oracle, n, horizon, M):
+    """General-N tiled kernel == oracle FP64 restatement per path."""
+    mu, sigma, w = _factor_case(n, 7 + n)
+    x = 0.02 * math.sqrt(horizon)
+    k, thr, seed = max(1, n // 10), -0.03, 99 + n
+    port = gpu.Portfolio(mu, sigma, w)
+    res, S, W = _run_paths(gpu, port, M, seed, x, k, thr, horizon=horizon)
+    L_ref, _ = oracle.cholesky_lower(sigma)
+    ref = oracle.mc_philox(mu, L_ref, w, horizon, M, seed, x, k, thr, want_S=True, want_port=True,
+                           want_R=True)
+    _assert_S_parity(S, ref["S"], ref["R"], x, max_near_frac=5e-2)
+    assert np.max(np.abs(W - ref["port"])) <= PORT_TOL
+    assert res["crash_count"] == int((S >= k).sum())
+    assert res["breach_count"] == int((W < thr).sum())
+
+
+def test_tiled_agrees_with_fused_for_small_n(gpu, monkeypatch):
+    """For N <= 64 the tiled kernel (forced) and the fused kernel draw the
+    same normals: S equal per path away from the threshold, w.R within FP32
+    tolerance."""
+    from riskgpu import synth
+    p = synth.one_factor_50(n_paths=1)
+    port = gpu.Portfolio(p.mu, p.sigma, p.weights)
+    M = 50000
+    monkeypatch.delenv("RG_PLAIN_KERNEL", raising=False)
+    r1, S1, W1 = _run_paths(gpu, port, M, 4, p.x, p.k, p.port_threshold, horizon=2)
+    monkeypatch.setenv("RG_PLAIN_KERNEL", "tiled")
+    r2, S2, W2 = _run_paths(gpu, port, M, 4, p.x, p.k, p.port_threshold, horizon=2)
+    assert np.max(np.abs(W1 - W2)) <= 1e-5
+    assert (S1 != S2).mean() < 1e-3
+
+
+@pytest.mark.parametrize("n", [20, 200])
+def test_aggregated_draws_parity(gpu, oracle, n):
+    """RG_DRAWS_AGGREGATED: one N(0,1) draw per asset times sqrt(H), per path
+    against the oracle's restatement of the same mode."""
+    mu, sigma, w = _factor_case(n, 3 + n, factors=1)
+    H, M, seed = 10, 5000, 17
+    x, k, thr = 0.06, max(1, n // 10), -0.05
+    port = gpu.Portfolio(mu, sigma, w)
+    torch = _torch()
+    S = torch.empty(M, dtype=torch.int32, device="cuda")
+    W = torch.empty(M, dtype=torch.float32, device="cuda")
+    q = gpu.make_query(M, seed, x=x, k=k, horizon=H, port_threshold=thr, d_s_values=S.data_ptr(),
+                       d_port_values=W.data_ptr(), draw_mode=gpu.DRAWS_AGGREGATED)
+    port.simulate(q)
+    torch.cuda.synchronize()
+    L_ref, _ = oracle.cholesky_lower(sigma)
+    ref = oracle.mc_philox(mu, L_ref, w, H, M, seed, x, k, thr, want_S=True, want_port=True, want_R=True,
+                           aggregated=True)
+    _assert_S_parity(S.cpu().numpy(), ref["S"], ref["R"], x, max_near_frac=5e-2)
+    assert np.max(np.abs(W.cpu().numpy() - ref["port"])) <= PORT_TOL
+
+
+def test_aggregated_statistics_match_daily(gpu, oracle):
+    """Both draw modes sample the same N(H w.mu, H w'Sigma w): breach
+    probabilities agree with the closed form within 3 SE."""
+    mu, sigma, w = _factor_case(120, 5)
+    port = gpu.Portfolio(mu, sigma, w)
+    M, H, thr = 4_000_000, 10, -0.04
+    cf = oracle.portfolio_closed_form(mu, sigma, w, H, thr, 0.99)
+    se = math.sqrt(cf["p_breach"] * (1 - cf["p_breach"]) / M)
+    for mode in (gpu.DRAWS_DAILY, gpu.DRAWS_AGGREGATED):
+        r = port.simulate(gpu.make_query(M, 8, x=0.1, k=12, horizon=H, port_threshold=thr, draw_mode=mode))
+        assert abs(r["p_breach"] - cf["p_breach"]) < 3 * se
+
+
+def test_tiled_var_exact(gpu, oracle):
+    r, W, _ = _var_case(gpu, 300_000, 0.99, n=150)
+    var, cvar, T = oracle.var_cvar(W, 0.99)
+    assert r["var"] == var and abs(r["cvar"] - cvar) <= 1e-9 * abs(cvar)
