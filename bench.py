@@ -43,7 +43,6 @@ import time
 ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, os.path.join(ROOT, "gpu-montecarlo-risk_gb300"))
 
-WORKLOAD = "one_factor_50"
 METRIC = "paths_per_second"
 UNIT = "paths/s"
 
@@ -58,10 +57,17 @@ def parse():
     ap.add_argument("--steps", type=int, default=30)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="riskgpu", choices=["riskgpu", "reference"])
-    ap.add_argument("--paths", type=int, default=100_000_000)
+    ap.add_argument("--paths", type=int, default=None,
+                    help="paths per step (default: the workload's, 1e8 or 1e7)")
     ap.add_argument("--cpu-seconds", type=float, default=12.0,
                     help="approximate CPU time of the bounded CPU samples")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--workload", default="one_factor_50",
+                    choices=["one_factor_50", "five_factor_600"],
+                    help="one_factor_50 is the headline; five_factor_600 (N=600, H=10, "
+                         "M=1e7 per step) is the precision-form workload")
+    ap.add_argument("--draw-mode", default="daily", choices=["daily", "aggregated"])
+    ap.add_argument("--precision", default="auto", choices=["auto", "fp32", "bf16x3"])
     return ap.parse_args()
 
 
@@ -72,10 +78,24 @@ def dist_env():
     return rank, world, local
 
 
-def config(args, world):
-    return {"workload": WORKLOAD, "n_assets": 50, "horizon_days": 1, "paths_per_step": args.paths,
-            "factor": "one-factor", "weights": "Dirichlet(1)", "port_threshold": -0.03,
-            "x": 0.03, "k": 5, "rng": "philox4x32-10", "precision": "fp32",
+def workload(args):
+    """The synthetic portfolio of the workload, sized to the paths per step."""
+    from riskgpu import synth
+    if args.workload == "five_factor_600":
+        if args.paths is None:
+            args.paths = 10_000_000
+        return synth.five_factor_600(n_paths=args.paths)
+    if args.paths is None:
+        args.paths = 100_000_000
+    return synth.one_factor_50(n_paths=args.paths)
+
+
+def config(args, world, p):
+    return {"workload": args.workload, "n_assets": p.n, "horizon_days": p.horizon,
+            "paths_per_step": args.paths,
+            "factor": "one-factor" if p.n == 50 else "five-factor", "weights": "Dirichlet(1)",
+            "port_threshold": p.port_threshold, "x": p.x, "k": p.k, "rng": "philox4x32-10",
+            "draws": args.draw_mode, "precision": args.precision,
             "cholesky": "fp64 on GPU, resident", "l2": "flushed (256 MB write) before each timed step",
             "parallelism": f"path-range shards x{world}" if world > 1 else "1 GPU"}
 
@@ -195,8 +215,7 @@ def reference_arm(args):
     rank, world, _ = dist_env()
     if rank != 0:
         return
-    from riskgpu import synth
-    p = synth.one_factor_50(n_paths=args.paths)
+    p = workload(args)
     threads = os.cpu_count() or 1
     times, kinds, details = [], None, None
     # warm-up + K timed steps, each a bounded sample of the workload
@@ -209,14 +228,14 @@ def reference_arm(args):
             kinds, details = kind, det
     value = statistics.median(times)
     best_model = max(details, key=lambda m: details[m]["paths_per_s"])
-    sample = (f"{details[best_model]['paths']} paths of the {WORKLOAD} workload per step with the "
+    sample = (f"{details[best_model]['paths']} paths of the {args.workload} workload per step with the "
               f"reference's {best_model} model ({details[best_model]['threads']} threads); "
               f"serial {details['serial']['paths_per_s']:.4g} paths/s, openmp "
               f"{details['openmp']['paths_per_s']:.4g} paths/s")
     line = {"impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * args.paths / value,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
-            "data": "synthetic", "config": config(args, world),
+            "data": "synthetic", "config": config(args, world, p),
             "cpu_baseline": {"value": value, "unit": UNIT, "cores": details[best_model]["threads"],
                              "kind": kinds, "sample": sample},
             "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
@@ -239,16 +258,18 @@ def engine_arm(args):
         if dist is not None:
             dist.barrier()
 
-    p = synth.one_factor_50(n_paths=args.paths)
+    p = workload(args)
     stream = torch.cuda.Stream()
     sp = stream.cuda_stream
     port = riskgpu.Portfolio(p.mu, p.sigma, p.weights)
     counts = torch.zeros(2, dtype=torch.int64, device="cuda")
     flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda")
     # shard: rank r owns paths [r*M, (r+1)*M)
-    q = riskgpu.make_query(args.paths, p.seed, x=p.x, k=p.k, horizon=1,
+    prec = {"auto": riskgpu.PREC_AUTO, "fp32": riskgpu.PREC_FP32, "bf16x3": riskgpu.PREC_BF16X3}[args.precision]
+    draws = riskgpu.DRAWS_AGGREGATED if args.draw_mode == "aggregated" else riskgpu.DRAWS_DAILY
+    q = riskgpu.make_query(args.paths, p.seed, x=p.x, k=p.k, horizon=p.horizon,
                            port_threshold=p.port_threshold, path_offset=rank * args.paths,
-                           precision=riskgpu.PREC_FP32)
+                           precision=prec, draw_mode=draws)
 
     with torch.cuda.stream(stream):
         for _ in range(args.warmup):
@@ -281,22 +302,32 @@ def engine_arm(args):
     value = world * args.paths * args.steps / (total_ms * 1e-3)
     ms_per_step = total_ms / args.steps
 
-    # ---- e2e through the reference-facing plugin call (host buffers)
-    call = riskgpu.PluginCall(p.mu, p.sigma)
+    # ---- e2e through the reference-facing plugin call (host buffers); the
+    # plugin API has no horizon or weights, so other workloads go through
+    # rg_run (host mu, Sigma, weights; the same copies, factorisation and
+    # kernel)
     e2e_steps = max(3, min(args.steps, 5))
     os.environ.pop("RG_MATERIALIZE_S", None)
     os.environ.pop("RG_RNG", None)
+    if args.workload == "one_factor_50":
+        call = riskgpu.PluginCall(p.mu, p.sigma)
+        run_once = lambda: call.run(args.paths, p.k, p.x, p.seed)["status"]
+        e2e_path = "get_cuda_model().run_model (host mu/Sigma)"
+    else:
+        qh = riskgpu.make_query(args.paths, p.seed, x=p.x, k=p.k, horizon=p.horizon,
+                                port_threshold=p.port_threshold, precision=prec, draw_mode=draws)
+        run_once = lambda: (riskgpu.run(p.mu, p.sigma, p.weights, qh), 0)[1]
+        e2e_path = "rg_run (host mu/Sigma/weights)"
     with quiet_stdout():
-        call.run(args.paths, p.k, p.x, p.seed)  # warm-up
+        run_once()  # warm-up
         barrier()
         t0 = time.perf_counter()
         for _ in range(e2e_steps):
-            r = call.run(args.paths, p.k, p.x, p.seed)
-            if r["status"] != 0:
-                raise RuntimeError("plugin call failed")
+            if run_once() != 0:
+                raise RuntimeError("end-to-end call failed")
         barrier()
         e2e_s = (time.perf_counter() - t0) / e2e_steps
-    h2d = 8 * p.n + 8 * p.n * p.n
+    h2d = 8 * p.n + 8 * p.n * p.n + (8 * p.n if args.workload != "one_factor_50" else 0)
     d2h = 16 + 4 + 16  # counts, Cholesky info, portfolio moments
 
     # ---- roofline of the fused kernel
@@ -304,11 +335,13 @@ def engine_arm(args):
     torch.cuda.synchronize()
     n = p.n
     flops_per_path = n * (n + 1) + 2 * n          # triangular contraction + w.R
-    normals_per_path = 4 * ((n + 3) // 4)          # one Philox block per 4 assets
+    days = 1 if args.draw_mode == "aggregated" else p.horizon
+    normals_per_path = 4 * ((n + 3) // 4) * days   # one Philox block per 4 assets and day
     achieved = flops_per_path * args.paths / (ms_per_step * 1e-3) / 1e12
     t_ideal = (flops_per_path / (peaks["fp32_tflops"] * 1e12)
                + normals_per_path / peaks["normals_per_s"]) * args.paths
-    roofline = {"bound": "alu", "kernel": "rg::mc_rows_kernel<13,true> (N=50)",
+    kname = ("rg::mc_rows_kernel<13,true,false> (N=50)" if n <= 64 else "rg::mc_tiled_kernel<false>")
+    roofline = {"bound": "alu", "kernel": kname,
                 "achieved": achieved, "peak": peaks["fp32_tflops"], "unit": "TFLOP/s",
                 "frac": achieved / peaks["fp32_tflops"],
                 "peak_source": "measured live: FP32 FMA micro-kernel (rg_probe_peaks)",
@@ -321,10 +354,9 @@ def engine_arm(args):
     line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": ms_per_step, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
-            "config": config(args, world),
+            "config": config(args, world, p),
             "e2e": {"value": world * args.paths / e2e_s, "unit": UNIT, "h2d_bytes_per_step": h2d,
-                    "d2h_bytes_per_step": d2h, "ms_per_step": 1e3 * e2e_s,
-                    "path": "get_cuda_model().run_model (host mu/Sigma)"},
+                    "d2h_bytes_per_step": d2h, "ms_per_step": 1e3 * e2e_s, "path": e2e_path},
             "gpu_launches": args.steps, "clocks": clk, "roofline": roofline,
             "wall_s_timed_region": wall, "counts_last_step": {"crash": crash, "breach": breach},
             "step_ms": [round(v, 4) for v in step_ms]}
@@ -332,7 +364,7 @@ def engine_arm(args):
         kind, det = run_cpu_reference(p, args.cpu_seconds, os.cpu_count() or 1)
         s = det["serial"]
         line["cpu_baseline"] = {"value": s["paths_per_s"], "unit": UNIT, "cores": 1, "kind": kind,
-                                "sample": f"{s['paths']} paths of {WORKLOAD}, reference serial model "
+                                "sample": f"{s['paths']} paths of {args.workload}, reference serial model "
                                           f"(MT19937 + polar normals + FP64 dgemv), 1 thread",
                                 "openmp_all_cores": {"value": det["openmp"]["paths_per_s"],
                                                      "cores": det["openmp"]["threads"]}}

@@ -128,6 +128,9 @@ static void portfolio_free(Portfolio *p)
     cudaFree(p->d_mu64);
     cudaFree(p->d_Lp);
     cudaFree(p->d_Lt);
+    cudaFree(p->d_tc[0]);
+    cudaFree(p->d_tc[1]);
+    cudaFree(p->d_err);
     cudaFree(p->d_w32);
     cudaFree(p->d_aux);
     cudaFree(p->d_info);
@@ -143,8 +146,13 @@ static int validate_query(const Portfolio *p, const rg_query *q)
     if (!std::isfinite(q->port_threshold)) return set_error(RG_ERR_INVALID, "port_threshold must be finite");
     if (q->rng != RG_RNG_PHILOX && q->rng != RG_RNG_XORWOW_REF)
         return set_error(RG_ERR_INVALID, "unknown rng layout %d", q->rng);
-    if (q->precision < RG_PREC_FP32 || q->precision > RG_PREC_AUTO)
+    if (q->precision < RG_PREC_FP32 || q->precision > RG_PREC_FP16X3)
         return set_error(RG_ERR_INVALID, "unknown precision %d", q->precision);
+    const bool tensor = q->precision == RG_PREC_BF16X3 || q->precision == RG_PREC_FP16X3;
+    if (tensor && q->rng != RG_RNG_PHILOX)
+        return set_error(RG_ERR_UNSUPPORTED, "the tensor-core form uses the Philox layout");
+    if (p && tensor && p->n > tc_max_n())
+        return set_error(RG_ERR_UNSUPPORTED, "the tensor-core form is limited to N <= %d (N = %d)", tc_max_n(), p->n);
     if (!(q->var_level >= 0.0 && q->var_level < 1.0))
         return set_error(RG_ERR_INVALID, "var_level must be in [0, 1)");
     if (q->draw_mode != RG_DRAWS_DAILY && q->draw_mode != RG_DRAWS_AGGREGATED)
@@ -185,6 +193,12 @@ static double inv_norm_cdf(double prob)
 static cudaError_t launch_counting(const Portfolio *p, const rg_query *q, const PlainArgs &a,
                                    int sm_count, cudaStream_t s)
 {
+    if (q->precision == RG_PREC_BF16X3 || q->precision == RG_PREC_FP16X3) {
+        const int bf16 = q->precision == RG_PREC_BF16X3 ? 1 : 0;
+        if (!p->d_tc[bf16] || !a.err) return cudaErrorInvalidValue; // prepared by the caller
+        return launch_tc(a, p->d_tc[bf16], bf16, q->draw_mode == RG_DRAWS_AGGREGATED, p->wmu, a.err,
+                         sm_count, s);
+    }
     if (q->rng == RG_RNG_PHILOX && (p->n > fused_max_n() || env_contains("RG_PLAIN_KERNEL", "tiled")))
         return launch_tiled(a, p->d_Lt, q->draw_mode == RG_DRAWS_AGGREGATED, sm_count, s);
     if (q->rng == RG_RNG_PHILOX && p->n <= fused_max_n() &&
@@ -248,6 +262,7 @@ static PlainArgs make_args(const Portfolio *p, const rg_query *q, unsigned long 
     a.s_values = q->d_s_values;
     a.port_values = q->d_port_values;
     a.counts = d_counts;
+    a.err = p->d_err;
     return a;
 }
 
@@ -343,7 +358,8 @@ int rg_portfolio_create(int32_t n, const double *mu, const double *sigma, int64_
     if (st) return st;
     const size_t nn = (size_t)n * n;
     const size_t need = nn * 8 * (dev_in ? 1 : 2) + (size_t)n * 24 + (size_t)packed_len(n) * 4 +
-                        (size_t)tiled_kpad(n) * tiled_npad(n) * 4 + 64;
+                        (size_t)tiled_kpad(n) * tiled_npad(n) * 4 +
+                        (n <= tc_max_n() ? 2 * tc_tile_bytes(n) : 0) + 64;
     st = admit(need);
     if (st) return st;
 
@@ -363,6 +379,11 @@ int rg_portfolio_create(int32_t n, const double *mu, const double *sigma, int64_
     RG_CUDA_TRY(cudaMalloc(&p->d_Lp, (size_t)packed_len(n) * sizeof(float)));
     if (n <= tiled_max_n())
         RG_CUDA_TRY(cudaMalloc(&p->d_Lt, (size_t)tiled_kpad(n) * tiled_npad(n) * sizeof(float)));
+    RG_CUDA_TRY(cudaMalloc(&p->d_err, sizeof(unsigned int)));
+    if (n <= tc_max_n()) {
+        RG_CUDA_TRY(cudaMalloc(&p->d_tc[0], tc_tile_bytes(n)));
+        RG_CUDA_TRY(cudaMalloc(&p->d_tc[1], tc_tile_bytes(n)));
+    }
     RG_CUDA_TRY(cudaMalloc(&p->d_w32, (size_t)n * sizeof(float)));
     RG_CUDA_TRY(cudaMalloc(&p->d_aux, 2 * sizeof(double)));
     RG_CUDA_TRY(cudaMalloc(&p->d_info, sizeof(int)));
@@ -403,6 +424,12 @@ int rg_portfolio_create(int32_t n, const double *mu, const double *sigma, int64_
     p->wsw = aux[0];
     p->wmu = aux[1];
     if (p->d_Lt) RG_CUDA_TRY(launch_build_lt(p->d_L64, n, p->d_Lt, s));
+    if (p->d_tc[0]) {
+        RG_CUDA_TRY(launch_build_tc_tiles(p->d_L64, p->d_w32, n, 0, p->d_tc[0], s));
+        RG_CUDA_TRY(launch_build_tc_tiles(p->d_L64, p->d_w32, n, 1, p->d_tc[1], s));
+    }
+    RG_CUDA_TRY(cudaMemsetAsync(p->d_err, 0, sizeof(unsigned int), s));
+    RG_CUDA_TRY(cudaStreamSynchronize(s));
     p->h_Lp.resize((size_t)packed_len(n));
     p->h_mu.resize((size_t)n);
     p->h_w.resize((size_t)n);
@@ -545,6 +572,14 @@ int rg_simulate(const rg_portfolio *h, const rg_query *q, rg_result *out, void *
     RG_CUDA_TRY(cudaStreamSynchronize(s));
     cudaEventElapsedTime(&ms, e0, e1);
     passes = 1;
+    if (q->precision == RG_PREC_BF16X3 || q->precision == RG_PREC_FP16X3) {
+        unsigned int err = 0;
+        RG_CUDA_TRY(cudaMemcpy(&err, p->d_err, sizeof(err), cudaMemcpyDeviceToHost));
+        if (err) {
+            st = set_error(RG_ERR_TIMEOUT, "tensor-core kernel gave up a bounded wait (error word 0x%x)", err);
+            goto fail;
+        }
+    }
     n_tail = (int64_t)tail[0];
     if (want_var && !(n_tail < T && T <= n_tail + (int64_t)ncand && ncand <= sc.cap)) {
         // The band missed the order statistic: histogram pass over
@@ -650,8 +685,6 @@ int rg_run(int32_t n, const double *mu, const double *sigma, int64_t ld, const d
 {
     int st = validate_query(nullptr, q);
     if (st) return st;
-    if (n > plain_small_max_n())
-        return set_error(RG_ERR_UNSUPPORTED, "N = %d exceeds this kernel's limit %d", n, plain_small_max_n());
     rg_portfolio *h = nullptr;
     st = rg_portfolio_create(n, mu, sigma, ld, weights, 0, &h);
     if (st) return st;

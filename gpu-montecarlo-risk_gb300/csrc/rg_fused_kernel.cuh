@@ -70,7 +70,8 @@ __device__ __forceinline__ void var_path(const PlainArgs &a, float port, unsigne
     const float t = (port - a.sel_lo) * a.sel_inv_w;
     const int b = (t < 0.f) ? -1 : (t >= (float)a.sel_bins ? a.sel_bins : (int)t);
     if (a.var_mode == 2) {
-        atomicAdd(&shist[b + 1], 1u);
+        if (shist) atomicAdd(&shist[b + 1], 1u);
+        else atomicAdd(&a.hist[b + 1], 1ull); // kernels without a shared histogram
         return;
     }
     if (b < a.sel_target) {
@@ -96,12 +97,12 @@ __device__ __forceinline__ void var_path(const PlainArgs &a, float port, unsigne
 // per counter, and the CTA's histogram merged into the global one.
 __device__ __forceinline__ void cta_flush(const PlainArgs &a, int crash, int breach, int n_tail,
                                           long long tail_fx, unsigned long long *sacc,
-                                          unsigned int *shist)
+                                          unsigned int *shist, bool var)
 {
     const int tid = threadIdx.x;
     crash = __reduce_add_sync(0xffffffffu, crash);
     breach = __reduce_add_sync(0xffffffffu, breach);
-    if (shist) {
+    if (var) {
         n_tail = __reduce_add_sync(0xffffffffu, n_tail);
 #pragma unroll
         for (int o = 16; o > 0; o >>= 1) tail_fx += __shfl_xor_sync(0xffffffffu, tail_fx, o);
@@ -109,7 +110,7 @@ __device__ __forceinline__ void cta_flush(const PlainArgs &a, int crash, int bre
     if ((tid & 31) == 0) {
         atomicAdd(&sacc[0], (unsigned long long)crash);
         atomicAdd(&sacc[1], (unsigned long long)breach);
-        if (shist) {
+        if (var) {
             atomicAdd(&sacc[2], (unsigned long long)n_tail);
             atomicAdd(&sacc[3], (unsigned long long)tail_fx);
         }
@@ -118,7 +119,7 @@ __device__ __forceinline__ void cta_flush(const PlainArgs &a, int crash, int bre
     if (tid == 0) {
         if (sacc[0]) atomicAdd(&a.counts[0], sacc[0]);
         if (sacc[1]) atomicAdd(&a.counts[1], sacc[1]);
-        if (shist && a.var_mode == 1) {
+        if (var && a.var_mode == 1) {
             if (sacc[2]) atomicAdd(&a.tail[0], sacc[2]);
             if (sacc[3]) atomicAdd(&a.tail[1], sacc[3]);
         }
@@ -194,7 +195,7 @@ __global__ void __launch_bounds__(kFusedThreads, 4) mc_rows_kernel(const PlainAr
         if (a.port_values) a.port_values[p] = port;
         if (VAR) var_path(a, port, shist, n_tail, tail_fx);
     }
-    cta_flush(a, crash, breach, n_tail, tail_fx, sacc, VAR ? shist : nullptr);
+    cta_flush(a, crash, breach, n_tail, tail_fx, sacc, VAR ? shist : nullptr, VAR);
 }
 
 template <int NQ>

@@ -115,6 +115,8 @@ struct Portfolio {
     double *d_mu64 = nullptr;  // n
     float *d_Lp = nullptr;     // packed rows (packed_len(n) floats)
     float *d_Lt = nullptr;     // L^T FP32 [tiled_kpad(n)][tiled_npad(n)], zero padded
+    unsigned char *d_tc[2] = {nullptr, nullptr}; // tensor-core tiles (FP16, BF16), N <= tc_max_n()
+    unsigned int *d_err = nullptr; // error word of the tensor-core kernel
     float *d_w32 = nullptr;    // n (zeros when no weights)
     double *d_aux = nullptr;   // [2]: w^T Sigma w, w.mu
     int *d_info = nullptr;
@@ -161,6 +163,7 @@ struct PlainArgs {
     unsigned int cand_cap;
     unsigned long long *tail;   // [0] tail paths, [1] sum of -w.R * 2^32 (int64 bits)
     unsigned long long *hist;   // [sel_bins + 2]
+    unsigned int *err;          // device error word of the tensor-core kernel (bounded waits)
 };
 
 // Shared-memory histogram size of the VaR pass: bins plus under/overflow.
@@ -178,6 +181,13 @@ cudaError_t launch_build_lt(const double *L64, int n, float *Lt, cudaStream_t s)
 int tiled_max_n();
 int tiled_npad(int n);
 int tiled_kpad(int n);
+// rg_mc_tc.cu: tcgen05 precision form (Philox layout), N <= tc_max_n().
+cudaError_t launch_tc(const PlainArgs &a, const unsigned char *tiles, int bf16, bool aggregated, double wmu,
+                      unsigned int *err, int sm_count, cudaStream_t s);
+cudaError_t launch_build_tc_tiles(const double *L64, const float *w32, int n, int bf16, unsigned char *tiles,
+                                  cudaStream_t s);
+int tc_max_n();
+size_t tc_tile_bytes(int n);
 // rg_mc_fused.cu: N <= 64 kernel, L in parameter space; Philox only.
 cudaError_t launch_fused(const PlainArgs &a, const float *Lp_host, const float *hmu, const float *w,
                          int sm_count, cudaStream_t s);

@@ -1,0 +1,481 @@
+// Precision form: the correlation step on tcgen05 tensor cores.
+//
+// Computes what the plain kernels compute (R = H mu + L Zsum per path, S,
+// w.R, crash / breach / VaR bookkeeping) with the contraction as a dense
+// MMA on sm_103a tensor cores, in transposed form so that a whole path
+// tile's normals fit on chip:
+//
+//     D[asset, path] = sum_k Lhat[asset, k] * Z[path, k]      (tcgen05.mma)
+//
+// M = 128 asset rows per MMA (n_mt = ceil((N+1)/128) row tiles), N = 64 paths
+// per tile, K = 16 per instruction, FP32 accumulators in tensor memory
+// (n_mt x 64 columns, <= 512).  Row N of Lhat is w^T L, so the portfolio
+// return w.R = H w.mu + D[N, path] comes out of the same MMAs.
+//
+// Precision: both operands are split into FP16 (or BF16) hi + lo parts and
+// three products are accumulated, Lhi.Zhi + Lhi.Zlo + Llo.Zhi (the lo.lo term
+// is below FP32 rounding for FP16).  L is scaled by 2^8 so its lo part stays
+// in FP16's normal range; the epilogue scales back exactly.
+//
+// Per CTA (one per SM, persistent over 64-path tiles):
+//   1. all 256 threads draw the tile's normals (engine Philox layout, summed
+//      over H days, or one sqrt(H)-scaled draw per asset in the aggregated
+//      mode), split them and store them in shared memory in the canonical
+//      K-major 128-byte-swizzled layout (one 64 x 64 block per K tile);
+//   2. one thread of warp 1 streams the pre-swizzled Lhat tiles (128 x 64,
+//      hi and lo, 32 KB) from HBM with cp.async.bulk into a 2-stage ring
+//      guarded by mbarriers; one thread of warp 0 issues the MMAs for each
+//      row tile over its K tiles (lower triangle: row tile m needs
+//      K < 128 (m + 1)) and commits each stage back to the producer;
+//   3. all warps read the accumulators with tcgen05.ld (warp w reads lanes
+//      32 (w % 4) .. +31, half the columns each), compare each asset's
+//      return with -x (ballot + popc per path) and collect w.R from row N.
+// Every wait is bounded: on expiry the kernel sets an error word, drains its
+// own copies and MMAs (again bounded), frees its tensor memory and returns;
+// the host reports RG_ERR_TIMEOUT.
+#include <cstdint>
+#include <cstring>
+#include <cuda_fp16.h>
+#include <cuda_bf16.h>
+#include "rg_fused_kernel.cuh"
+
+namespace rg {
+
+static constexpr int kTcPaths = 64;        // N of the MMA: paths per tile
+static constexpr int kTcRows = 128;        // M of the MMA: asset rows per row tile
+static constexpr int kTcKt = 64;           // K elements per shared-memory tile (128 B)
+static constexpr int kTcThreads = 256;
+static constexpr int kTcMaxKt = 10;        // K tiles of Z kept on chip (N <= 640)
+static constexpr int kTcStages = 2;
+static constexpr int kTcTileBytes = kTcRows * kTcKt * 2;  // one part of an Lhat tile: 16 KB
+static constexpr int kTcZBytes = kTcPaths * kTcKt * 2;    // one part of a Z K tile: 8 KB
+static constexpr float kTcLScale = 256.0f;
+static constexpr unsigned kTcSpinLimit = 1u << 26;        // try_wait polls before giving up
+static constexpr unsigned long long kTcWaitNs = 2000000000ull; // 2 s of wall time
+
+struct TcArgs {
+    PlainArgs a;
+    const unsigned char *tiles; // [n_mt][n_kt][2][16 KB] pre-swizzled Lhat (hi, lo)
+    int n_mt;                   // row tiles
+    int n_kt;                   // K tiles
+    int bf16;                   // operand type: 0 FP16, 1 BF16
+    int aggregated;
+    float sqrt_h;
+    double hwmu;                // H w.mu
+    unsigned int *err;          // device error word
+};
+
+// ------------------------------------------------------------ PTX wrappers
+__device__ __forceinline__ uint32_t smem_u32(const void *p) { return (uint32_t)__cvta_generic_to_shared(p); }
+
+__device__ __forceinline__ void mbar_init(uint64_t *bar, unsigned count)
+{
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(bar)), "r"(count));
+}
+__device__ __forceinline__ void mbar_expect_tx(uint64_t *bar, unsigned bytes)
+{
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar)), "r"(bytes)
+                 : "memory");
+}
+__device__ __forceinline__ bool mbar_try_wait(uint64_t *bar, unsigned parity)
+{
+    uint32_t ok;
+    asm volatile("{\n\t.reg .pred p;\n\t"
+                 "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+                 "selp.u32 %0, 1, 0, p;\n\t}"
+                 : "=r"(ok)
+                 : "r"(smem_u32(bar)), "r"(parity)
+                 : "memory");
+    return ok != 0;
+}
+__device__ __forceinline__ unsigned long long global_ns()
+{
+    unsigned long long t;
+    asm volatile("mov.u64 %0, %globaltimer;" : "=l"(t));
+    return t;
+}
+// Bounded wait: gives up (returns false) after kTcWaitNs of wall time or
+// kTcSpinLimit polls, whichever comes first.
+__device__ __forceinline__ bool mbar_wait(uint64_t *bar, unsigned parity)
+{
+    const unsigned long long t0 = global_ns();
+    for (unsigned i = 0; i < kTcSpinLimit; i++) {
+        if (mbar_try_wait(bar, parity)) return true;
+        if ((i & 255u) == 255u && global_ns() - t0 > kTcWaitNs) return false;
+    }
+    return false;
+}
+__device__ __forceinline__ void bulk_copy(void *smem_dst, const void *gmem_src, unsigned bytes, uint64_t *bar)
+{
+    asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
+                     smem_u32(smem_dst)),
+                 "l"(gmem_src), "r"(bytes), "r"(smem_u32(bar))
+                 : "memory");
+}
+__device__ __forceinline__ void fence_async_shared() { asm volatile("fence.proxy.async.shared::cta;" ::: "memory"); }
+__device__ __forceinline__ void tc_fence_before() { asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory"); }
+__device__ __forceinline__ void tc_fence_after() { asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory"); }
+
+// Shared-memory matrix descriptor: K-major, 128-byte swizzle, 8-row groups
+// 1024 bytes apart.
+__device__ __forceinline__ uint64_t sw128_desc(uint32_t addr)
+{
+    uint64_t d = 0;
+    d |= (uint64_t)((addr & 0x3FFFFu) >> 4);  // start address
+    d |= (uint64_t)1 << 16;                   // leading byte offset (unused by this layout)
+    d |= (uint64_t)(1024 >> 4) << 32;         // stride byte offset: next 8-row group
+    d |= (uint64_t)1 << 46;                   // descriptor version
+    d |= (uint64_t)2 << 61;                   // 128-byte swizzle
+    return d;
+}
+
+// Instruction descriptor of kind::f16: FP32 accumulator, A and B of the same
+// type (FP16 or BF16), both K-major, M x N.
+__host__ __device__ constexpr uint32_t tc_idesc(int bf16, int M, int N)
+{
+    return (1u << 4) | ((uint32_t)bf16 << 7) | ((uint32_t)bf16 << 10) | ((uint32_t)(N >> 3) << 17) |
+           ((uint32_t)(M >> 4) << 24);
+}
+
+__device__ __forceinline__ void tc_mma(uint32_t d_tmem, uint64_t a_desc, uint64_t b_desc, uint32_t idesc,
+                                       uint32_t accumulate)
+{
+    asm volatile("{\n\t.reg .pred p;\n\t"
+                 "setp.ne.b32 p, %4, 0;\n\t"
+                 "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n\t}" ::"r"(d_tmem),
+                 "l"(a_desc), "l"(b_desc), "r"(idesc), "r"(accumulate));
+}
+__device__ __forceinline__ void tc_commit(uint64_t *bar)
+{
+    asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(smem_u32(bar))
+                 : "memory");
+}
+
+// Byte offset of element (row r, k) in a K-major 128B-swizzled block of
+// 2-byte elements, 64 elements per row.
+__host__ __device__ __forceinline__ uint32_t sw128_offset(int r, int k)
+{
+    const int chunk = (k >> 3) ^ (r & 7);
+    return (uint32_t)((r >> 3) * 1024 + (r & 7) * 128 + chunk * 16 + (k & 7) * 2);
+}
+
+__device__ __forceinline__ void split2(float v, int bf16, unsigned short &hi, unsigned short &lo)
+{
+    if (bf16) {
+        const __nv_bfloat16 h = __float2bfloat16_rn(v);
+        const __nv_bfloat16 l = __float2bfloat16_rn(v - __bfloat162float(h));
+        hi = __bfloat16_as_ushort(h);
+        lo = __bfloat16_as_ushort(l);
+    } else {
+        const __half h = __float2half_rn(v);
+        const __half l = __float2half_rn(v - __half2float(h));
+        hi = __half_as_ushort(h);
+        lo = __half_as_ushort(l);
+    }
+}
+
+template <bool VAR>
+__global__ void __launch_bounds__(kTcThreads, 1) mc_tc_kernel(const TcArgs t)
+{
+    extern __shared__ __align__(1024) unsigned char tc_smem[];
+    // layout (dynamic): [Z hi: n_kt x 8 KB][Z lo: n_kt x 8 KB][stages x (hi 16 KB, lo 16 KB)]
+    const PlainArgs &a = t.a;
+    unsigned char *base = (unsigned char *)(((uintptr_t)tc_smem + 1023) & ~(uintptr_t)1023);
+    unsigned char *zhi = base;
+    unsigned char *zlo = zhi + t.n_kt * kTcZBytes;
+    unsigned char *lst = zlo + t.n_kt * kTcZBytes;
+
+    __shared__ __align__(8) uint64_t full_bar[kTcStages], empty_bar[kTcStages], done_bar;
+    __shared__ uint32_t tmem_base_sh;
+    __shared__ int sS[kTcPaths];
+    __shared__ float sPort[kTcPaths];
+    __shared__ int s_abort;
+    __shared__ unsigned long long sacc[4];
+
+    const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+    const int n = a.n;
+    const int nq = (n + 3) >> 2;
+    const int ncols = 512;
+
+    if (tid < 4) sacc[tid] = 0ull;
+    if (tid == 0) {
+        for (int s = 0; s < kTcStages; s++) {
+            mbar_init(&full_bar[s], 1);
+            mbar_init(&empty_bar[s], 1);
+        }
+        mbar_init(&done_bar, 1);
+        s_abort = 0;
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    }
+    if (warp == 0) {
+        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(&tmem_base_sh)),
+                     "r"(ncols));
+        asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;");
+    }
+    tc_fence_before();
+    __syncthreads();
+    tc_fence_after();
+    const uint32_t tmem = tmem_base_sh;
+
+    int crash = 0, breach = 0, n_tail = 0;
+    long long tail_fx = 0;
+    const uint32_t idesc = tc_idesc(t.bf16, kTcRows, kTcPaths);
+    // pipeline state (kept across tiles)
+    unsigned prod_iter = 0, cons_iter = 0, tile_iter = 0;
+    const long long ntiles = (a.n_paths + kTcPaths - 1) / kTcPaths;
+
+    for (long long tile = blockIdx.x; tile < ntiles; tile += gridDim.x, tile_iter++) {
+        if (s_abort) break;
+        const long long p0 = tile * kTcPaths;
+        // ---- 1. normals -> swizzled hi/lo Z tiles
+        {
+            const int p = tid & (kTcPaths - 1), r = tid >> 6;
+            const unsigned long long path = a.path0 + (unsigned long long)(p0 + p);
+            const uint32_t plo = (uint32_t)path, phi = (uint32_t)(path >> 32);
+            const int kq = t.n_kt * (kTcKt / 4);
+            for (int q = r; q < kq; q += 4) {
+                float z[4] = {0.f, 0.f, 0.f, 0.f};
+                if (q < nq) {
+                    const int days = t.aggregated ? 1 : a.horizon;
+                    for (int d = 0; d < days; d++) {
+                        const uint4 wv = rg_philox(make_uint4((uint32_t)(d * nq + q), 0u, plo, phi), a.keys);
+                        float z0, z1, z2, z3;
+                        rg_box_muller(wv.x, wv.y, z0, z1);
+                        rg_box_muller(wv.z, wv.w, z2, z3);
+                        z[0] += z0;
+                        z[1] += z1;
+                        z[2] += z2;
+                        z[3] += z3;
+                    }
+                    if (t.aggregated)
+                        for (int e = 0; e < 4; e++) z[e] *= t.sqrt_h;
+                }
+                unsigned short h[4], l[4];
+                for (int e = 0; e < 4; e++) split2(z[e], t.bf16, h[e], l[e]);
+                const int k = 4 * q, kt = k / kTcKt, kk = k % kTcKt;
+                const uint32_t off = (uint32_t)kt * kTcZBytes + sw128_offset(p, kk);
+                const uint2 hv = make_uint2((uint32_t)h[0] | ((uint32_t)h[1] << 16), (uint32_t)h[2] | ((uint32_t)h[3] << 16));
+                const uint2 lv = make_uint2((uint32_t)l[0] | ((uint32_t)l[1] << 16), (uint32_t)l[2] | ((uint32_t)l[3] << 16));
+                *reinterpret_cast<uint2 *>(zhi + off) = hv;
+                *reinterpret_cast<uint2 *>(zlo + off) = lv;
+            }
+        }
+        if (tid < kTcPaths) {
+            sS[tid] = 0;
+            sPort[tid] = 0.f;
+        }
+        fence_async_shared(); // generic-proxy writes of Z -> visible to the tensor cores
+        tc_fence_before();
+        __syncthreads();
+        tc_fence_after();
+
+        // ---- 2. producer (warp 1, one thread) and MMA issuer (warp 0, one thread)
+        if (warp == 1 && lane == 0) {
+            for (int mt = 0; mt < t.n_mt; mt++) {
+                const int kend = min(t.n_kt, (kTcRows * (mt + 1) + kTcKt - 1) / kTcKt);
+                const int kts = (mt == t.n_mt - 1) ? t.n_kt : kend;
+                for (int kt = 0; kt < kts; kt++, prod_iter++) {
+                    const int s = prod_iter % kTcStages;
+                    const unsigned ph = ((prod_iter / kTcStages) & 1u) ^ 1u;
+                    if (!mbar_wait(&empty_bar[s], ph)) {
+                        atomicOr(t.err, 1u);
+                        s_abort = 1;
+                        break;
+                    }
+                    mbar_expect_tx(&full_bar[s], 2 * kTcTileBytes);
+                    const unsigned char *src = t.tiles + ((size_t)(mt * t.n_kt + kt) * 2) * kTcTileBytes;
+                    unsigned char *dst = lst + (size_t)s * 2 * kTcTileBytes;
+                    bulk_copy(dst, src, kTcTileBytes, &full_bar[s]);
+                    bulk_copy(dst + kTcTileBytes, src + kTcTileBytes, kTcTileBytes, &full_bar[s]);
+                }
+                if (s_abort) break;
+            }
+        } else if (warp == 0 && lane == 0) {
+            for (int mt = 0; mt < t.n_mt; mt++) {
+                const int kend = min(t.n_kt, (kTcRows * (mt + 1) + kTcKt - 1) / kTcKt);
+                const int kts = (mt == t.n_mt - 1) ? t.n_kt : kend;
+                const uint32_t d_tmem = tmem + (uint32_t)(mt * kTcPaths);
+                for (int kt = 0; kt < kts; kt++, cons_iter++) {
+                    const int s = cons_iter % kTcStages;
+                    const unsigned ph = (cons_iter / kTcStages) & 1u;
+                    if (s_abort || !mbar_wait(&full_bar[s], ph)) {
+                        atomicOr(t.err, 2u);
+                        s_abort = 1;
+                        break;
+                    }
+                    tc_fence_after();
+                    const uint32_t lhi = smem_u32(lst + (size_t)s * 2 * kTcTileBytes);
+                    const uint32_t llo = lhi + kTcTileBytes;
+                    const uint32_t zh = smem_u32(zhi + (size_t)kt * kTcZBytes);
+                    const uint32_t zl = smem_u32(zlo + (size_t)kt * kTcZBytes);
+#pragma unroll
+                    for (int ks = 0; ks < kTcKt / 16; ks++) {
+                        const uint32_t o = (uint32_t)ks * 32; // 16 elements = 32 bytes along K
+                        const uint32_t acc0 = (kt > 0 || ks > 0) ? 1u : 0u;
+                        tc_mma(d_tmem, sw128_desc(lhi + o), sw128_desc(zh + o), idesc, acc0);
+                        tc_mma(d_tmem, sw128_desc(lhi + o), sw128_desc(zl + o), idesc, 1u);
+                        tc_mma(d_tmem, sw128_desc(llo + o), sw128_desc(zh + o), idesc, 1u);
+                    }
+                    tc_commit(&empty_bar[s]); // stage free once these MMAs complete
+                }
+                if (s_abort) break;
+            }
+            tc_commit(&done_bar); // all MMAs of the tile issued so far
+        }
+        // ---- 3. epilogue
+        const bool done_ok = mbar_wait(&done_bar, tile_iter & 1u);
+        if (!done_ok && tid == 0) {
+            atomicOr(t.err, 4u);
+            s_abort = 1;
+        }
+        tc_fence_after();
+        if (done_ok && !s_abort) {
+            const int quarter = warp & 3, half = warp >> 2;
+            for (int mt = 0; mt < t.n_mt; mt++) {
+                const int row = mt * kTcRows + quarter * 32 + lane; // this thread's asset row
+                const uint32_t taddr = tmem + ((uint32_t)(quarter * 32) << 16) + (uint32_t)(mt * kTcPaths + half * 32);
+                uint32_t v[32];
+                asm volatile("tcgen05.ld.sync.aligned.32x32b.x32.b32 "
+                             "{%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15,"
+                             "%16,%17,%18,%19,%20,%21,%22,%23,%24,%25,%26,%27,%28,%29,%30,%31}, [%32];"
+                             : "=r"(v[0]), "=r"(v[1]), "=r"(v[2]), "=r"(v[3]), "=r"(v[4]), "=r"(v[5]),
+                               "=r"(v[6]), "=r"(v[7]), "=r"(v[8]), "=r"(v[9]), "=r"(v[10]), "=r"(v[11]),
+                               "=r"(v[12]), "=r"(v[13]), "=r"(v[14]), "=r"(v[15]), "=r"(v[16]), "=r"(v[17]),
+                               "=r"(v[18]), "=r"(v[19]), "=r"(v[20]), "=r"(v[21]), "=r"(v[22]), "=r"(v[23]),
+                               "=r"(v[24]), "=r"(v[25]), "=r"(v[26]), "=r"(v[27]), "=r"(v[28]), "=r"(v[29]),
+                               "=r"(v[30]), "=r"(v[31])
+                             : "r"(taddr));
+                asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+                // threshold on the scaled accumulator: D/2^8 < -x - H mu_i
+                const bool asset = row < n;
+                const float thr = asset ? (float)(((double)a.neg_x - (double)a.horizon * a.mu64[row]) * kTcLScale)
+                                        : 0.f;
+                int cnt = 0;
+#pragma unroll
+                for (int c = 0; c < 32; c++) {
+                    const float d = __uint_as_float(v[c]);
+                    const unsigned m = __ballot_sync(0xffffffffu, asset && d < thr);
+                    if (lane == c) cnt = __popc(m);
+                }
+                if (cnt) atomicAdd(&sS[half * 32 + lane], cnt);
+                if (row == n) {
+#pragma unroll
+                    for (int c = 0; c < 32; c++)
+                        sPort[half * 32 + c] = (float)(t.hwmu + (double)(__uint_as_float(v[c]) * (1.0f / kTcLScale)));
+                }
+            }
+        }
+        tc_fence_before();
+        __syncthreads();
+        if (!s_abort && tid < kTcPaths) {
+            const long long p = p0 + tid;
+            if (p < a.n_paths) {
+                const int S = sS[tid];
+                const float port = sPort[tid];
+                crash += (S >= a.k) ? 1 : 0;
+                breach += (a.has_w && port < a.port_thr) ? 1 : 0;
+                if (a.s_values) a.s_values[p] = S;
+                if (a.port_values) a.port_values[p] = port;
+                if (VAR) var_path(a, port, nullptr, n_tail, tail_fx); // histogram pass: global atomics
+            }
+        }
+        __syncthreads();
+        tc_fence_after();
+    }
+
+    // ---- teardown: drain in-flight copies and MMAs (bounded), free TMEM
+    if (s_abort) {
+        if (warp == 0 && lane == 0) {
+            tc_commit(&done_bar);
+            mbar_wait(&done_bar, tile_iter & 1u);
+        }
+        if (warp == 1 && lane == 0) {
+            for (unsigned i = cons_iter; i < prod_iter; i++)
+                mbar_wait(&full_bar[i % kTcStages], (i / kTcStages) & 1u);
+        }
+    }
+    tc_fence_before();
+    __syncthreads();
+    tc_fence_after();
+    if (warp == 0) asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(ncols));
+    cta_flush(a, crash, breach, n_tail, tail_fx, sacc, nullptr, VAR);
+}
+
+// Pre-swizzled Lhat tiles: rows 0..N-1 = L (lower triangle), row N = w^T L,
+// scaled by 2^8, split into hi and lo (FP16 or BF16), each (row tile, K tile)
+// block laid out exactly as the kernel's shared memory expects.
+__global__ void build_tc_tiles_kernel(const double *L, const float *w, int n, int n_mt, int n_kt, int bf16,
+                                      unsigned char *tiles)
+{
+    const long long total = (long long)n_mt * kTcRows * n_kt * kTcKt;
+    for (long long idx = blockIdx.x * (long long)blockDim.x + threadIdx.x; idx < total;
+         idx += (long long)gridDim.x * blockDim.x) {
+        const int col = (int)(idx % (n_kt * kTcKt));
+        const int row = (int)(idx / (n_kt * kTcKt));
+        double v = 0.0;
+        if (col < n) {
+            if (row < n) {
+                if (col <= row) v = L[(long long)row * n + col];
+            } else if (row == n) {
+                for (int i = col; i < n; i++) v += (double)w[i] * L[(long long)i * n + col];
+            }
+        }
+        const float f = (float)(v * kTcLScale);
+        unsigned short hi, lo;
+        if (bf16) {
+            const __nv_bfloat16 h = __float2bfloat16_rn(f);
+            hi = __bfloat16_as_ushort(h);
+            lo = __bfloat16_as_ushort(__float2bfloat16_rn(f - __bfloat162float(h)));
+        } else {
+            const __half h = __float2half_rn(f);
+            hi = __half_as_ushort(h);
+            lo = __half_as_ushort(__float2half_rn(f - __half2float(h)));
+        }
+        const int mt = row / kTcRows, r = row % kTcRows, kt = col / kTcKt, k = col % kTcKt;
+        const size_t blk = ((size_t)(mt * n_kt + kt) * 2) * kTcTileBytes;
+        const uint32_t off = sw128_offset(r, k);
+        *reinterpret_cast<unsigned short *>(tiles + blk + off) = hi;
+        *reinterpret_cast<unsigned short *>(tiles + blk + kTcTileBytes + off) = lo;
+    }
+}
+
+int tc_max_n() { return kTcMaxKt * kTcKt; }
+int tc_row_tiles(int n) { return (n + 1 + kTcRows - 1) / kTcRows; }
+int tc_k_tiles(int n) { return (n + kTcKt - 1) / kTcKt; }
+size_t tc_tile_bytes(int n) { return (size_t)tc_row_tiles(n) * tc_k_tiles(n) * 2 * kTcTileBytes; }
+
+cudaError_t launch_build_tc_tiles(const double *L64, const float *w32, int n, int bf16, unsigned char *tiles,
+                                  cudaStream_t s)
+{
+    build_tc_tiles_kernel<<<256, 256, 0, s>>>(L64, w32, n, tc_row_tiles(n), tc_k_tiles(n), bf16, tiles);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_tc(const PlainArgs &a, const unsigned char *tiles, int bf16, bool aggregated, double wmu,
+                      unsigned int *err, int sm_count, cudaStream_t s)
+{
+    if (a.n > tc_max_n()) return cudaErrorInvalidValue;
+    TcArgs t;
+    memset(&t, 0, sizeof(t));
+    t.a = a;
+    t.tiles = tiles;
+    t.n_mt = tc_row_tiles(a.n);
+    t.n_kt = tc_k_tiles(a.n);
+    t.bf16 = bf16;
+    t.aggregated = aggregated ? 1 : 0;
+    t.sqrt_h = sqrtf((float)a.horizon);
+    t.hwmu = (double)a.horizon * wmu;
+    t.err = err;
+    if (t.n_mt * kTcPaths > 512) return cudaErrorInvalidValue;
+    const size_t smem = 1024 + (size_t)t.n_kt * 2 * kTcZBytes + (size_t)kTcStages * 2 * kTcTileBytes;
+    auto kern = (a.var_mode != 0) ? mc_tc_kernel<true> : mc_tc_kernel<false>;
+    cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e != cudaSuccess) return e;
+    long long tiles_n = (a.n_paths + kTcPaths - 1) / kTcPaths;
+    long long grid = sm_count;
+    if (tiles_n < grid) grid = tiles_n;
+    kern<<<(unsigned)grid, kTcThreads, smem, s>>>(t);
+    return cudaGetLastError();
+}
+
+} // namespace rg

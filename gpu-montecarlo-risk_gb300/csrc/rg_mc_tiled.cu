@@ -214,7 +214,7 @@ __global__ void __launch_bounds__(kTiledThreads, 1) mc_tiled_kernel(const TiledA
         }
         __syncthreads();
     }
-    cta_flush(a, crash, breach, n_tail, tail_fx, sacc, VAR ? shist : nullptr);
+    cta_flush(a, crash, breach, n_tail, tail_fx, sacc, VAR ? shist : nullptr, VAR);
 }
 
 int tiled_max_n() { return 768; }

@@ -32,6 +32,7 @@ DRAWS_AGGREGATED = 1
 PREC_FP32 = 0
 PREC_BF16X3 = 1
 PREC_AUTO = 2
+PREC_FP16X3 = 3
 INPUT_DEVICE = 0x1
 
 # Every symbol include/riskgpu.h and include/riskgpu_plugin.h declare.

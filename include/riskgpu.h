@@ -64,9 +64,12 @@ typedef enum {
 
 /* Arithmetic of the correlation step R = H mu + L Zsum. */
 typedef enum {
-    RG_PREC_FP32 = 0,   /* FP32 FMA cores (the plain fused kernel) */
-    RG_PREC_BF16X3 = 1, /* tcgen05 tensor cores, BF16 hi+lo split of Z and L, FP32 accumulate */
-    RG_PREC_AUTO = 2    /* the engine picks by asset count */
+    RG_PREC_FP32 = 0,   /* FP32 FMA cores (the plain fused kernels) */
+    RG_PREC_BF16X3 = 1, /* tcgen05 tensor cores: BF16 hi+lo split of Z and L, three products,
+                           FP32 accumulation (about 2^-16 relative per product) */
+    RG_PREC_AUTO = 2,   /* the engine picks (currently the FP32 kernels) */
+    RG_PREC_FP16X3 = 3  /* tcgen05 tensor cores: FP16 hi+lo split (L scaled by 2^8), three
+                           products, FP32 accumulation (close to FP32 rounding) */
 } rg_precision;
 
 /* Flags for rg_portfolio_create. */
