@@ -67,7 +67,7 @@ def parse():
                     help="one_factor_50 is the headline; five_factor_600 (N=600, H=10, "
                          "M=1e7 per step) is the precision-form workload")
     ap.add_argument("--draw-mode", default="daily", choices=["daily", "aggregated"])
-    ap.add_argument("--precision", default="auto", choices=["auto", "fp32", "bf16x3"])
+    ap.add_argument("--precision", default="auto", choices=["auto", "fp32", "bf16x3", "fp16x3"])
     return ap.parse_args()
 
 
@@ -265,7 +265,8 @@ def engine_arm(args):
     counts = torch.zeros(2, dtype=torch.int64, device="cuda")
     flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda")
     # shard: rank r owns paths [r*M, (r+1)*M)
-    prec = {"auto": riskgpu.PREC_AUTO, "fp32": riskgpu.PREC_FP32, "bf16x3": riskgpu.PREC_BF16X3}[args.precision]
+    prec = {"auto": riskgpu.PREC_AUTO, "fp32": riskgpu.PREC_FP32, "bf16x3": riskgpu.PREC_BF16X3,
+            "fp16x3": riskgpu.PREC_FP16X3}[args.precision]
     draws = riskgpu.DRAWS_AGGREGATED if args.draw_mode == "aggregated" else riskgpu.DRAWS_DAILY
     q = riskgpu.make_query(args.paths, p.seed, x=p.x, k=p.k, horizon=p.horizon,
                            port_threshold=p.port_threshold, path_offset=rank * args.paths,

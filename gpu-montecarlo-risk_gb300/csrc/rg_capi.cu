@@ -195,9 +195,13 @@ static cudaError_t launch_counting(const Portfolio *p, const rg_query *q, const 
 {
     if (q->precision == RG_PREC_BF16X3 || q->precision == RG_PREC_FP16X3) {
         const int bf16 = q->precision == RG_PREC_BF16X3 ? 1 : 0;
-        if (!p->d_tc[bf16] || !a.err) return cudaErrorInvalidValue; // prepared by the caller
+        if (!p->d_tc[bf16] || !a.err) return cudaErrorInvalidValue; // prepared at creation
+        const cudaError_t e = cudaMemsetAsync(a.err, 0, sizeof(unsigned int), s);
+        if (e != cudaSuccess) return e;
+        // RG_FAULT_INJECT=tcstall: one pipeline stage is never filled, so the
+        // kernel's bounded wait runs out (host-side injection; no fault)
         return launch_tc(a, p->d_tc[bf16], bf16, q->draw_mode == RG_DRAWS_AGGREGATED, p->wmu, a.err,
-                         sm_count, s);
+                         env_contains("RG_FAULT_INJECT", "tcstall"), sm_count, s);
     }
     if (q->rng == RG_RNG_PHILOX && (p->n > fused_max_n() || env_contains("RG_PLAIN_KERNEL", "tiled")))
         return launch_tiled(a, p->d_Lt, q->draw_mode == RG_DRAWS_AGGREGATED, sm_count, s);

@@ -183,7 +183,7 @@ int tiled_npad(int n);
 int tiled_kpad(int n);
 // rg_mc_tc.cu: tcgen05 precision form (Philox layout), N <= tc_max_n().
 cudaError_t launch_tc(const PlainArgs &a, const unsigned char *tiles, int bf16, bool aggregated, double wmu,
-                      unsigned int *err, int sm_count, cudaStream_t s);
+                      unsigned int *err, bool inject_stall, int sm_count, cudaStream_t s);
 cudaError_t launch_build_tc_tiles(const double *L64, const float *w32, int n, int bf16, unsigned char *tiles,
                                   cudaStream_t s);
 int tc_max_n();

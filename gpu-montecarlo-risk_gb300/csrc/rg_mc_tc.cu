@@ -18,7 +18,7 @@
 // in FP16's normal range; the epilogue scales back exactly.
 //
 // Per CTA (one per SM, persistent over 64-path tiles):
-//   1. all 256 threads draw the tile's normals (engine Philox layout, summed
+//   1. all 512 threads draw the tile's normals (engine Philox layout, summed
 //      over H days, or one sqrt(H)-scaled draw per asset in the aggregated
 //      mode), split them and store them in shared memory in the canonical
 //      K-major 128-byte-swizzled layout (one 64 x 64 block per K tile);
@@ -27,9 +27,10 @@
 //      guarded by mbarriers; one thread of warp 0 issues the MMAs for each
 //      row tile over its K tiles (lower triangle: row tile m needs
 //      K < 128 (m + 1)) and commits each stage back to the producer;
-//   3. all warps read the accumulators with tcgen05.ld (warp w reads lanes
-//      32 (w % 4) .. +31, half the columns each), compare each asset's
-//      return with -x (ballot + popc per path) and collect w.R from row N.
+//   3. all 16 warps read the accumulators with tcgen05.ld (warp w reads
+//      lanes 32 (w % 4) .. +31 and a quarter of the columns), compare each
+//      asset's return with -x (ballot + popc per path) and collect w.R from
+//      row N.
 // Every wait is bounded: on expiry the kernel sets an error word, drains its
 // own copies and MMAs (again bounded), frees its tensor memory and returns;
 // the host reports RG_ERR_TIMEOUT.
@@ -44,7 +45,7 @@ namespace rg {
 static constexpr int kTcPaths = 64;        // N of the MMA: paths per tile
 static constexpr int kTcRows = 128;        // M of the MMA: asset rows per row tile
 static constexpr int kTcKt = 64;           // K elements per shared-memory tile (128 B)
-static constexpr int kTcThreads = 256;
+static constexpr int kTcThreads = 512;
 static constexpr int kTcMaxKt = 10;        // K tiles of Z kept on chip (N <= 640)
 static constexpr int kTcStages = 2;
 static constexpr int kTcTileBytes = kTcRows * kTcKt * 2;  // one part of an Lhat tile: 16 KB
@@ -63,6 +64,7 @@ struct TcArgs {
     float sqrt_h;
     double hwmu;                // H w.mu
     unsigned int *err;          // device error word
+    int inject_stall;           // host-side fault injection: one stage is never filled
 };
 
 // ------------------------------------------------------------ PTX wrappers
@@ -190,6 +192,7 @@ __global__ void __launch_bounds__(kTcThreads, 1) mc_tc_kernel(const TcArgs t)
     __shared__ int sS[kTcPaths];
     __shared__ float sPort[kTcPaths];
     __shared__ int s_abort;
+    __shared__ unsigned s_cons; // stages the MMA thread has consumed (for the abort drain)
     __shared__ unsigned long long sacc[4];
 
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
@@ -205,6 +208,7 @@ __global__ void __launch_bounds__(kTcThreads, 1) mc_tc_kernel(const TcArgs t)
         }
         mbar_init(&done_bar, 1);
         s_abort = 0;
+        s_cons = 0;
         asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
     }
     if (warp == 0) {
@@ -229,11 +233,11 @@ __global__ void __launch_bounds__(kTcThreads, 1) mc_tc_kernel(const TcArgs t)
         const long long p0 = tile * kTcPaths;
         // ---- 1. normals -> swizzled hi/lo Z tiles
         {
-            const int p = tid & (kTcPaths - 1), r = tid >> 6;
+            const int p = tid & (kTcPaths - 1), r = tid >> 6; // kTcThreads / 64 threads per path
             const unsigned long long path = a.path0 + (unsigned long long)(p0 + p);
             const uint32_t plo = (uint32_t)path, phi = (uint32_t)(path >> 32);
             const int kq = t.n_kt * (kTcKt / 4);
-            for (int q = r; q < kq; q += 4) {
+            for (int q = r; q < kq; q += kTcThreads / kTcPaths) {
                 float z[4] = {0.f, 0.f, 0.f, 0.f};
                 if (q < nq) {
                     const int days = t.aggregated ? 1 : a.horizon;
@@ -282,6 +286,7 @@ __global__ void __launch_bounds__(kTcThreads, 1) mc_tc_kernel(const TcArgs t)
                         s_abort = 1;
                         break;
                     }
+                    if (t.inject_stall && prod_iter == 1) continue; // never filled: the consumer's wait runs out
                     mbar_expect_tx(&full_bar[s], 2 * kTcTileBytes);
                     const unsigned char *src = t.tiles + ((size_t)(mt * t.n_kt + kt) * 2) * kTcTileBytes;
                     unsigned char *dst = lst + (size_t)s * 2 * kTcTileBytes;
@@ -321,6 +326,7 @@ __global__ void __launch_bounds__(kTcThreads, 1) mc_tc_kernel(const TcArgs t)
                 if (s_abort) break;
             }
             tc_commit(&done_bar); // all MMAs of the tile issued so far
+            s_cons = cons_iter;
         }
         // ---- 3. epilogue
         const bool done_ok = mbar_wait(&done_bar, tile_iter & 1u);
@@ -330,20 +336,16 @@ __global__ void __launch_bounds__(kTcThreads, 1) mc_tc_kernel(const TcArgs t)
         }
         tc_fence_after();
         if (done_ok && !s_abort) {
-            const int quarter = warp & 3, half = warp >> 2;
+            const int quarter = warp & 3, sub = warp >> 2; // lanes 32*quarter.., columns 16*sub..
             for (int mt = 0; mt < t.n_mt; mt++) {
                 const int row = mt * kTcRows + quarter * 32 + lane; // this thread's asset row
-                const uint32_t taddr = tmem + ((uint32_t)(quarter * 32) << 16) + (uint32_t)(mt * kTcPaths + half * 32);
-                uint32_t v[32];
-                asm volatile("tcgen05.ld.sync.aligned.32x32b.x32.b32 "
-                             "{%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15,"
-                             "%16,%17,%18,%19,%20,%21,%22,%23,%24,%25,%26,%27,%28,%29,%30,%31}, [%32];"
+                const uint32_t taddr = tmem + ((uint32_t)(quarter * 32) << 16) + (uint32_t)(mt * kTcPaths + sub * 16);
+                uint32_t v[16];
+                asm volatile("tcgen05.ld.sync.aligned.32x32b.x16.b32 "
+                             "{%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, [%16];"
                              : "=r"(v[0]), "=r"(v[1]), "=r"(v[2]), "=r"(v[3]), "=r"(v[4]), "=r"(v[5]),
                                "=r"(v[6]), "=r"(v[7]), "=r"(v[8]), "=r"(v[9]), "=r"(v[10]), "=r"(v[11]),
-                               "=r"(v[12]), "=r"(v[13]), "=r"(v[14]), "=r"(v[15]), "=r"(v[16]), "=r"(v[17]),
-                               "=r"(v[18]), "=r"(v[19]), "=r"(v[20]), "=r"(v[21]), "=r"(v[22]), "=r"(v[23]),
-                               "=r"(v[24]), "=r"(v[25]), "=r"(v[26]), "=r"(v[27]), "=r"(v[28]), "=r"(v[29]),
-                               "=r"(v[30]), "=r"(v[31])
+                               "=r"(v[12]), "=r"(v[13]), "=r"(v[14]), "=r"(v[15])
                              : "r"(taddr));
                 asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
                 // threshold on the scaled accumulator: D/2^8 < -x - H mu_i
@@ -352,16 +354,16 @@ __global__ void __launch_bounds__(kTcThreads, 1) mc_tc_kernel(const TcArgs t)
                                         : 0.f;
                 int cnt = 0;
 #pragma unroll
-                for (int c = 0; c < 32; c++) {
+                for (int c = 0; c < 16; c++) {
                     const float d = __uint_as_float(v[c]);
                     const unsigned m = __ballot_sync(0xffffffffu, asset && d < thr);
                     if (lane == c) cnt = __popc(m);
                 }
-                if (cnt) atomicAdd(&sS[half * 32 + lane], cnt);
+                if (lane < 16 && cnt) atomicAdd(&sS[sub * 16 + lane], cnt);
                 if (row == n) {
 #pragma unroll
-                    for (int c = 0; c < 32; c++)
-                        sPort[half * 32 + c] = (float)(t.hwmu + (double)(__uint_as_float(v[c]) * (1.0f / kTcLScale)));
+                    for (int c = 0; c < 16; c++)
+                        sPort[sub * 16 + c] = (float)(t.hwmu + (double)(__uint_as_float(v[c]) * (1.0f / kTcLScale)));
                 }
             }
         }
@@ -390,7 +392,8 @@ __global__ void __launch_bounds__(kTcThreads, 1) mc_tc_kernel(const TcArgs t)
             mbar_wait(&done_bar, tile_iter & 1u);
         }
         if (warp == 1 && lane == 0) {
-            for (unsigned i = cons_iter; i < prod_iter; i++)
+            // copies issued but not consumed: wait for them to land
+            for (unsigned i = s_cons; i < prod_iter; i++)
                 mbar_wait(&full_bar[i % kTcStages], (i / kTcStages) & 1u);
         }
     }
@@ -452,7 +455,7 @@ cudaError_t launch_build_tc_tiles(const double *L64, const float *w32, int n, in
 }
 
 cudaError_t launch_tc(const PlainArgs &a, const unsigned char *tiles, int bf16, bool aggregated, double wmu,
-                      unsigned int *err, int sm_count, cudaStream_t s)
+                      unsigned int *err, bool inject_stall, int sm_count, cudaStream_t s)
 {
     if (a.n > tc_max_n()) return cudaErrorInvalidValue;
     TcArgs t;
@@ -466,6 +469,7 @@ cudaError_t launch_tc(const PlainArgs &a, const unsigned char *tiles, int bf16, 
     t.sqrt_h = sqrtf((float)a.horizon);
     t.hwmu = (double)a.horizon * wmu;
     t.err = err;
+    t.inject_stall = inject_stall ? 1 : 0;
     if (t.n_mt * kTcPaths > 512) return cudaErrorInvalidValue;
     const size_t smem = 1024 + (size_t)t.n_kt * 2 * kTcZBytes + (size_t)kTcStages * 2 * kTcTileBytes;
     auto kern = (a.var_mode != 0) ? mc_tc_kernel<true> : mc_tc_kernel<false>;

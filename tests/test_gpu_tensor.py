@@ -53,3 +53,56 @@ def test_tc_per_path_parity(gpu, oracle, prec, n, horizon, M):
     assert not bad.any(), f"{int(bad.sum())} paths differ; first {np.nonzero(bad)[0][:5]}"
     assert r["crash_count"] == int((S >= k).sum())
     assert r["breach_count"] == int((W < thr).sum())
+
+
+def test_tc_bounded_wait_reports_timeout(gpu, monkeypatch):
+    """Failure detection without a GPU fault: with RG_FAULT_INJECT=tcstall
+    one pipeline stage is never filled, the kernel's bounded wait (2 s) runs
+    out, it drains its own copies and MMAs, frees its tensor memory and sets
+    its error word; the host returns RG_ERR_TIMEOUT and the context stays
+    usable for the next query."""
+    mu, sigma, w = _case(200, 3)
+    port = gpu.Portfolio(mu, sigma, w)
+    q = gpu.make_query(4096, 1, x=0.02, k=5, precision=3)
+    monkeypatch.setenv("RG_FAULT_INJECT", "tcstall")
+    with pytest.raises(gpu.RiskGpuError) as e:
+        port.simulate(q)
+    assert e.value.status == gpu.RG_ERR_TIMEOUT
+    monkeypatch.delenv("RG_FAULT_INJECT")
+    r = port.simulate(q)
+    assert r["n_paths"] == 4096
+
+
+@pytest.mark.parametrize("prec", ["fp16x3", "bf16x3"])
+def test_tc_var_and_aggregated(gpu, oracle, prec):
+    """VaR/CVaR order statistics of the tensor-core form equal those of its
+    own per-path returns; aggregated draws match the oracle per path."""
+    code, near_tol, port_tol = CASES[prec]
+    mu, sigma, w = _case(300, 11)
+    port = gpu.Portfolio(mu, sigma, w)
+    r, S, W = _run(gpu, port, 200_000, 3, 0.05, 30, -0.04, 5, code, var_level=0.99)
+    var, cvar, T = oracle.var_cvar(W, 0.99)
+    assert r["tail_count"] == T and r["var"] == var and abs(r["cvar"] - cvar) <= 1e-9 * abs(cvar)
+    M = 2000
+    r, S, W = _run(gpu, port, M, 9, 0.05, 30, -0.04, 5, code, draw_mode=1)
+    L_ref, _ = oracle.cholesky_lower(sigma)
+    ref = oracle.mc_philox(mu, L_ref, w, 5, M, 9, 0.05, 30, -0.04, want_S=True, want_port=True, want_R=True,
+                           aggregated=True)
+    assert np.max(np.abs(W - ref["port"])) <= port_tol
+    near = np.min(np.abs(ref["R"] + 0.05), axis=1) < near_tol
+    assert not ((S != ref["S"]) & ~near).any()
+
+
+def test_tc_statistics_vs_fp32_and_closed_form(gpu, oracle):
+    """All forms agree: the tensor-core estimate of the breach probability
+    is within 3 SE of the FP64 closed form at N = 600, H = 10."""
+    from riskgpu import synth
+    p = synth.five_factor_600(n_paths=1)
+    port = gpu.Portfolio(p.mu, p.sigma, p.weights)
+    M = 2_000_000
+    cf = oracle.portfolio_closed_form(p.mu, p.sigma, p.weights, p.horizon, p.port_threshold, 0.99)
+    se = math.sqrt(cf["p_breach"] * (1 - cf["p_breach"]) / M)
+    for prec in (0, 1, 3):
+        r = port.simulate(gpu.make_query(M, 21, x=p.x, k=p.k, horizon=p.horizon,
+                                         port_threshold=p.port_threshold, precision=prec))
+        assert abs(r["p_breach"] - cf["p_breach"]) < 3 * se, (prec, r["p_breach"], cf["p_breach"])
