@@ -188,6 +188,18 @@ cudaError_t launch_build_tc_tiles(const double *L64, const float *w32, int n, in
                                   cudaStream_t s);
 int tc_max_n();
 size_t tc_tile_bytes(int n);
+// batches of (portfolio, query) items in one persistent launch
+void tc_fill_batch_item(void *item_out, const PlainArgs &a, const unsigned char *tiles, int bf16,
+                        bool aggregated, double wmu, long long tile_begin);
+size_t tc_item_bytes();
+long long tc_tiles_of(long long n_paths);
+int tc_row_tiles_of(int n);
+int tc_k_tiles_of(int n);
+cudaError_t launch_tc_batch(const void *d_items, int n_items, long long total_tiles, int unit_tiles,
+                            unsigned int *work, unsigned int *err, int n_kt_max, int n_mt_max, int grid,
+                            cudaStream_t s);
+cudaError_t tc_batch_prepare();
+int tc_batch_occupancy(int n_kt_max);
 // rg_mc_fused.cu: N <= 64 kernel, L in parameter space; Philox only.
 cudaError_t launch_fused(const PlainArgs &a, const float *Lp_host, const float *hmu, const float *w,
                          int sm_count, cudaStream_t s);

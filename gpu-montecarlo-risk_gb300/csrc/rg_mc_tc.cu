@@ -54,17 +54,36 @@ static constexpr float kTcLScale = 256.0f;
 static constexpr unsigned kTcSpinLimit = 1u << 26;        // try_wait polls before giving up
 static constexpr unsigned long long kTcWaitNs = 2000000000ull; // 2 s of wall time
 
-struct TcArgs {
-    PlainArgs a;
-    const unsigned char *tiles; // [n_mt][n_kt][2][16 KB] pre-swizzled Lhat (hi, lo)
-    int n_mt;                   // row tiles
-    int n_kt;                   // K tiles
-    int bf16;                   // operand type: 0 FP16, 1 BF16
-    int aggregated;
-    float sqrt_h;
-    double hwmu;                // H w.mu
-    unsigned int *err;          // device error word
-    int inject_stall;           // host-side fault injection: one stage is never filled
+// One (portfolio, query) of a launch.  Tiles of 64 paths are numbered
+// globally across the items of a launch; item i owns tiles
+// [tile_begin, tile_begin + ceil(n_paths / 64)).
+struct TcItem {
+    const unsigned char *tiles;   // pre-swizzled Lhat of the portfolio
+    const double *mu64;           // daily means
+    unsigned long long *counts;   // [2] crash, breach of this item
+    int *s_values;                // optional per-path outputs (item-local)
+    float *port_values;
+    unsigned long long path0;     // first path index of the query
+    long long n_paths;
+    long long tile_begin;
+    PhiloxKeys keys;
+    double hwmu;                  // H w.mu
+    int n, n_mt, n_kt, horizon, k, has_w, aggregated, bf16;
+    float neg_x, port_thr, sqrt_h, pad_;
+};
+
+struct TcBatch {
+    const TcItem *items;      // device array (batches), or null: use `one`
+    TcItem one;               // single item passed by value
+    int n_items;
+    int unit_tiles;           // tiles per work unit
+    long long total_tiles;
+    unsigned int *work;       // unit counter (dynamic scheduling), or null: static
+    unsigned int *err;        // device error word
+    int inject_stall;         // host-side fault injection: one stage is never filled
+    int n_kt_max;             // K tiles of the largest item (shared-memory size)
+    int tmem_cols;            // tensor-memory columns allocated (power of 2 >= 64 n_mt_max)
+    PlainArgs var;            // VaR fields of a single-item query (var_mode 0 otherwise)
 };
 
 // ------------------------------------------------------------ PTX wrappers
@@ -177,15 +196,15 @@ __device__ __forceinline__ void split2(float v, int bf16, unsigned short &hi, un
 }
 
 template <bool VAR>
-__global__ void __launch_bounds__(kTcThreads, 1) mc_tc_kernel(const TcArgs t)
+__global__ void __launch_bounds__(kTcThreads, 1) mc_tc_kernel(const __grid_constant__ TcBatch b)
 {
     extern __shared__ __align__(1024) unsigned char tc_smem[];
-    // layout (dynamic): [Z hi: n_kt x 8 KB][Z lo: n_kt x 8 KB][stages x (hi 16 KB, lo 16 KB)]
-    const PlainArgs &a = t.a;
+    // layout (dynamic): [Z hi: n_kt_max x 8 KB][Z lo: n_kt_max x 8 KB][stages x (hi 16 KB, lo 16 KB)]
+    const PlainArgs &a = b.var; // VaR fields (single-item queries)
     unsigned char *base = (unsigned char *)(((uintptr_t)tc_smem + 1023) & ~(uintptr_t)1023);
     unsigned char *zhi = base;
-    unsigned char *zlo = zhi + t.n_kt * kTcZBytes;
-    unsigned char *lst = zlo + t.n_kt * kTcZBytes;
+    unsigned char *zlo = zhi + b.n_kt_max * kTcZBytes;
+    unsigned char *lst = zlo + b.n_kt_max * kTcZBytes;
 
     __shared__ __align__(8) uint64_t full_bar[kTcStages], empty_bar[kTcStages], done_bar;
     __shared__ uint32_t tmem_base_sh;
@@ -193,12 +212,11 @@ __global__ void __launch_bounds__(kTcThreads, 1) mc_tc_kernel(const TcArgs t)
     __shared__ float sPort[kTcPaths];
     __shared__ int s_abort;
     __shared__ unsigned s_cons; // stages the MMA thread has consumed (for the abort drain)
+    __shared__ long long s_unit;
     __shared__ unsigned long long sacc[4];
 
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
-    const int n = a.n;
-    const int nq = (n + 3) >> 2;
-    const int ncols = 512;
+    const int ncols = b.tmem_cols;
 
     if (tid < 4) sacc[tid] = 0ull;
     if (tid == 0) {
@@ -221,168 +239,194 @@ __global__ void __launch_bounds__(kTcThreads, 1) mc_tc_kernel(const TcArgs t)
     tc_fence_after();
     const uint32_t tmem = tmem_base_sh;
 
-    int crash = 0, breach = 0, n_tail = 0;
+    int n_tail = 0;
     long long tail_fx = 0;
-    const uint32_t idesc = tc_idesc(t.bf16, kTcRows, kTcPaths);
     // pipeline state (kept across tiles)
     unsigned prod_iter = 0, cons_iter = 0, tile_iter = 0;
-    const long long ntiles = (a.n_paths + kTcPaths - 1) / kTcPaths;
+    const long long total = b.total_tiles;
 
-    for (long long tile = blockIdx.x; tile < ntiles; tile += gridDim.x, tile_iter++) {
-        if (s_abort) break;
-        const long long p0 = tile * kTcPaths;
-        // ---- 1. normals -> swizzled hi/lo Z tiles
-        {
-            const int p = tid & (kTcPaths - 1), r = tid >> 6; // kTcThreads / 64 threads per path
-            const unsigned long long path = a.path0 + (unsigned long long)(p0 + p);
-            const uint32_t plo = (uint32_t)path, phi = (uint32_t)(path >> 32);
-            const int kq = t.n_kt * (kTcKt / 4);
-            for (int q = r; q < kq; q += kTcThreads / kTcPaths) {
-                float z[4] = {0.f, 0.f, 0.f, 0.f};
-                if (q < nq) {
-                    const int days = t.aggregated ? 1 : a.horizon;
-                    for (int d = 0; d < days; d++) {
-                        const uint4 wv = rg_philox(make_uint4((uint32_t)(d * nq + q), 0u, plo, phi), a.keys);
-                        float z0, z1, z2, z3;
-                        rg_box_muller(wv.x, wv.y, z0, z1);
-                        rg_box_muller(wv.z, wv.w, z2, z3);
-                        z[0] += z0;
-                        z[1] += z1;
-                        z[2] += z2;
-                        z[3] += z3;
-                    }
-                    if (t.aggregated)
-                        for (int e = 0; e < 4; e++) z[e] *= t.sqrt_h;
-                }
-                unsigned short h[4], l[4];
-                for (int e = 0; e < 4; e++) split2(z[e], t.bf16, h[e], l[e]);
-                const int k = 4 * q, kt = k / kTcKt, kk = k % kTcKt;
-                const uint32_t off = (uint32_t)kt * kTcZBytes + sw128_offset(p, kk);
-                const uint2 hv = make_uint2((uint32_t)h[0] | ((uint32_t)h[1] << 16), (uint32_t)h[2] | ((uint32_t)h[3] << 16));
-                const uint2 lv = make_uint2((uint32_t)l[0] | ((uint32_t)l[1] << 16), (uint32_t)l[2] | ((uint32_t)l[3] << 16));
-                *reinterpret_cast<uint2 *>(zhi + off) = hv;
-                *reinterpret_cast<uint2 *>(zlo + off) = lv;
-            }
-        }
-        if (tid < kTcPaths) {
-            sS[tid] = 0;
-            sPort[tid] = 0.f;
-        }
-        fence_async_shared(); // generic-proxy writes of Z -> visible to the tensor cores
-        tc_fence_before();
+    for (long long round = 0;; round++) {
+        // claim a work unit: dynamic (atomic counter) for batches, static otherwise
         __syncthreads();
-        tc_fence_after();
+        if (tid == 0) s_unit = b.work ? (long long)atomicAdd(b.work, 1u) : blockIdx.x + round * gridDim.x;
+        __syncthreads();
+        const long long unit = s_unit;
+        if (s_abort || unit * b.unit_tiles >= total) break;
+        const long long tend = min(total, (unit + 1) * b.unit_tiles);
+        for (long long tile = unit * b.unit_tiles; tile < tend; tile++, tile_iter++) {
+            if (s_abort) break;
+            // the item of this tile (items are ordered by tile_begin)
+            int lo = 0, hi = b.n_items - 1;
+            const TcItem *items = b.items ? b.items : &b.one;
+            while (lo < hi) {
+                const int mid = (lo + hi + 1) >> 1;
+                if (items[mid].tile_begin <= tile) lo = mid; else hi = mid - 1;
+            }
+            const TcItem &it = items[lo];
+            const int n = it.n, nq = (n + 3) >> 2, n_kt = it.n_kt, n_mt = it.n_mt;
+            const long long p0 = (tile - it.tile_begin) * kTcPaths; // first path of the tile (item-local)
+            // ---- 1. normals -> swizzled hi/lo Z tiles
+            {
+                const int p = tid & (kTcPaths - 1), r = tid >> 6; // kTcThreads / 64 threads per path
+                const unsigned long long path = it.path0 + (unsigned long long)(p0 + p);
+                const uint32_t plo = (uint32_t)path, phi = (uint32_t)(path >> 32);
+                const int kq = n_kt * (kTcKt / 4);
+                for (int q = r; q < kq; q += kTcThreads / kTcPaths) {
+                    float z[4] = {0.f, 0.f, 0.f, 0.f};
+                    if (q < nq) {
+                        const int days = it.aggregated ? 1 : it.horizon;
+                        for (int d = 0; d < days; d++) {
+                            const uint4 wv = rg_philox(make_uint4((uint32_t)(d * nq + q), 0u, plo, phi), it.keys);
+                            float z0, z1, z2, z3;
+                            rg_box_muller(wv.x, wv.y, z0, z1);
+                            rg_box_muller(wv.z, wv.w, z2, z3);
+                            z[0] += z0;
+                            z[1] += z1;
+                            z[2] += z2;
+                            z[3] += z3;
+                        }
+                        if (it.aggregated)
+                            for (int e = 0; e < 4; e++) z[e] *= it.sqrt_h;
+                    }
+                    unsigned short h[4], l[4];
+                    for (int e = 0; e < 4; e++) split2(z[e], it.bf16, h[e], l[e]);
+                    const int k = 4 * q, kt = k / kTcKt, kk = k % kTcKt;
+                    const uint32_t off = (uint32_t)kt * kTcZBytes + sw128_offset(p, kk);
+                    const uint2 hv = make_uint2((uint32_t)h[0] | ((uint32_t)h[1] << 16), (uint32_t)h[2] | ((uint32_t)h[3] << 16));
+                    const uint2 lv = make_uint2((uint32_t)l[0] | ((uint32_t)l[1] << 16), (uint32_t)l[2] | ((uint32_t)l[3] << 16));
+                    *reinterpret_cast<uint2 *>(zhi + off) = hv;
+                    *reinterpret_cast<uint2 *>(zlo + off) = lv;
+                }
+            }
+            if (tid < kTcPaths) {
+                sS[tid] = 0;
+                sPort[tid] = 0.f;
+            }
+            fence_async_shared(); // generic-proxy writes of Z -> visible to the tensor cores
+            tc_fence_before();
+            __syncthreads();
+            tc_fence_after();
 
-        // ---- 2. producer (warp 1, one thread) and MMA issuer (warp 0, one thread)
-        if (warp == 1 && lane == 0) {
-            for (int mt = 0; mt < t.n_mt; mt++) {
-                const int kend = min(t.n_kt, (kTcRows * (mt + 1) + kTcKt - 1) / kTcKt);
-                const int kts = (mt == t.n_mt - 1) ? t.n_kt : kend;
-                for (int kt = 0; kt < kts; kt++, prod_iter++) {
-                    const int s = prod_iter % kTcStages;
-                    const unsigned ph = ((prod_iter / kTcStages) & 1u) ^ 1u;
-                    if (!mbar_wait(&empty_bar[s], ph)) {
-                        atomicOr(t.err, 1u);
-                        s_abort = 1;
-                        break;
+            // ---- 2. producer (warp 1, one thread) and MMA issuer (warp 0, one thread)
+            if (warp == 1 && lane == 0) {
+                for (int mt = 0; mt < n_mt; mt++) {
+                    const int kend = min(n_kt, (kTcRows * (mt + 1) + kTcKt - 1) / kTcKt);
+                    const int kts = (mt == n_mt - 1) ? n_kt : kend;
+                    for (int kt = 0; kt < kts; kt++, prod_iter++) {
+                        const int s = prod_iter % kTcStages;
+                        const unsigned ph = ((prod_iter / kTcStages) & 1u) ^ 1u;
+                        if (!mbar_wait(&empty_bar[s], ph)) {
+                            atomicOr(b.err, 1u);
+                            s_abort = 1;
+                            break;
+                        }
+                        if (b.inject_stall && prod_iter == 1) continue; // never filled: the consumer's wait runs out
+                        mbar_expect_tx(&full_bar[s], 2 * kTcTileBytes);
+                        const unsigned char *src = it.tiles + ((size_t)(mt * n_kt + kt) * 2) * kTcTileBytes;
+                        unsigned char *dst = lst + (size_t)s * 2 * kTcTileBytes;
+                        bulk_copy(dst, src, kTcTileBytes, &full_bar[s]);
+                        bulk_copy(dst + kTcTileBytes, src + kTcTileBytes, kTcTileBytes, &full_bar[s]);
                     }
-                    if (t.inject_stall && prod_iter == 1) continue; // never filled: the consumer's wait runs out
-                    mbar_expect_tx(&full_bar[s], 2 * kTcTileBytes);
-                    const unsigned char *src = t.tiles + ((size_t)(mt * t.n_kt + kt) * 2) * kTcTileBytes;
-                    unsigned char *dst = lst + (size_t)s * 2 * kTcTileBytes;
-                    bulk_copy(dst, src, kTcTileBytes, &full_bar[s]);
-                    bulk_copy(dst + kTcTileBytes, src + kTcTileBytes, kTcTileBytes, &full_bar[s]);
+                    if (s_abort) break;
                 }
-                if (s_abort) break;
-            }
-        } else if (warp == 0 && lane == 0) {
-            for (int mt = 0; mt < t.n_mt; mt++) {
-                const int kend = min(t.n_kt, (kTcRows * (mt + 1) + kTcKt - 1) / kTcKt);
-                const int kts = (mt == t.n_mt - 1) ? t.n_kt : kend;
-                const uint32_t d_tmem = tmem + (uint32_t)(mt * kTcPaths);
-                for (int kt = 0; kt < kts; kt++, cons_iter++) {
-                    const int s = cons_iter % kTcStages;
-                    const unsigned ph = (cons_iter / kTcStages) & 1u;
-                    if (s_abort || !mbar_wait(&full_bar[s], ph)) {
-                        atomicOr(t.err, 2u);
-                        s_abort = 1;
-                        break;
+            } else if (warp == 0 && lane == 0) {
+                const uint32_t idesc = tc_idesc(it.bf16, kTcRows, kTcPaths);
+                for (int mt = 0; mt < n_mt; mt++) {
+                    const int kend = min(n_kt, (kTcRows * (mt + 1) + kTcKt - 1) / kTcKt);
+                    const int kts = (mt == n_mt - 1) ? n_kt : kend;
+                    const uint32_t d_tmem = tmem + (uint32_t)(mt * kTcPaths);
+                    for (int kt = 0; kt < kts; kt++, cons_iter++) {
+                        const int s = cons_iter % kTcStages;
+                        const unsigned ph = (cons_iter / kTcStages) & 1u;
+                        if (s_abort || !mbar_wait(&full_bar[s], ph)) {
+                            atomicOr(b.err, 2u);
+                            s_abort = 1;
+                            break;
+                        }
+                        tc_fence_after();
+                        const uint32_t lhi = smem_u32(lst + (size_t)s * 2 * kTcTileBytes);
+                        const uint32_t llo = lhi + kTcTileBytes;
+                        const uint32_t zh = smem_u32(zhi + (size_t)kt * kTcZBytes);
+                        const uint32_t zl = smem_u32(zlo + (size_t)kt * kTcZBytes);
+#pragma unroll
+                        for (int ks = 0; ks < kTcKt / 16; ks++) {
+                            const uint32_t o = (uint32_t)ks * 32; // 16 elements = 32 bytes along K
+                            const uint32_t acc0 = (kt > 0 || ks > 0) ? 1u : 0u;
+                            tc_mma(d_tmem, sw128_desc(lhi + o), sw128_desc(zh + o), idesc, acc0);
+                            tc_mma(d_tmem, sw128_desc(lhi + o), sw128_desc(zl + o), idesc, 1u);
+                            tc_mma(d_tmem, sw128_desc(llo + o), sw128_desc(zh + o), idesc, 1u);
+                        }
+                        tc_commit(&empty_bar[s]); // stage free once these MMAs complete
                     }
-                    tc_fence_after();
-                    const uint32_t lhi = smem_u32(lst + (size_t)s * 2 * kTcTileBytes);
-                    const uint32_t llo = lhi + kTcTileBytes;
-                    const uint32_t zh = smem_u32(zhi + (size_t)kt * kTcZBytes);
-                    const uint32_t zl = smem_u32(zlo + (size_t)kt * kTcZBytes);
+                    if (s_abort) break;
+                }
+                tc_commit(&done_bar); // all MMAs of the tile issued so far
+                s_cons = cons_iter;
+            }
+            // ---- 3. epilogue
+            const bool done_ok = mbar_wait(&done_bar, tile_iter & 1u);
+            if (!done_ok && tid == 0) {
+                atomicOr(b.err, 4u);
+                s_abort = 1;
+            }
+            tc_fence_after();
+            if (done_ok && !s_abort) {
+                const int quarter = warp & 3, sub = warp >> 2; // lanes 32*quarter.., columns 16*sub..
+                for (int mt = 0; mt < n_mt; mt++) {
+                    const int row = mt * kTcRows + quarter * 32 + lane; // this thread's asset row
+                    const uint32_t taddr = tmem + ((uint32_t)(quarter * 32) << 16) + (uint32_t)(mt * kTcPaths + sub * 16);
+                    uint32_t v[16];
+                    asm volatile("tcgen05.ld.sync.aligned.32x32b.x16.b32 "
+                                 "{%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, [%16];"
+                                 : "=r"(v[0]), "=r"(v[1]), "=r"(v[2]), "=r"(v[3]), "=r"(v[4]), "=r"(v[5]),
+                                   "=r"(v[6]), "=r"(v[7]), "=r"(v[8]), "=r"(v[9]), "=r"(v[10]), "=r"(v[11]),
+                                   "=r"(v[12]), "=r"(v[13]), "=r"(v[14]), "=r"(v[15])
+                                 : "r"(taddr));
+                    asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+                    // threshold on the scaled accumulator: D/2^8 < -x - H mu_i
+                    const bool asset = row < n;
+                    const float thr = asset ? (float)(((double)it.neg_x - (double)it.horizon * it.mu64[row]) * kTcLScale)
+                                            : 0.f;
+                    int cnt = 0;
 #pragma unroll
-                    for (int ks = 0; ks < kTcKt / 16; ks++) {
-                        const uint32_t o = (uint32_t)ks * 32; // 16 elements = 32 bytes along K
-                        const uint32_t acc0 = (kt > 0 || ks > 0) ? 1u : 0u;
-                        tc_mma(d_tmem, sw128_desc(lhi + o), sw128_desc(zh + o), idesc, acc0);
-                        tc_mma(d_tmem, sw128_desc(lhi + o), sw128_desc(zl + o), idesc, 1u);
-                        tc_mma(d_tmem, sw128_desc(llo + o), sw128_desc(zh + o), idesc, 1u);
+                    for (int c = 0; c < 16; c++) {
+                        const float d = __uint_as_float(v[c]);
+                        const unsigned m = __ballot_sync(0xffffffffu, asset && d < thr);
+                        if (lane == c) cnt = __popc(m);
                     }
-                    tc_commit(&empty_bar[s]); // stage free once these MMAs complete
-                }
-                if (s_abort) break;
-            }
-            tc_commit(&done_bar); // all MMAs of the tile issued so far
-            s_cons = cons_iter;
-        }
-        // ---- 3. epilogue
-        const bool done_ok = mbar_wait(&done_bar, tile_iter & 1u);
-        if (!done_ok && tid == 0) {
-            atomicOr(t.err, 4u);
-            s_abort = 1;
-        }
-        tc_fence_after();
-        if (done_ok && !s_abort) {
-            const int quarter = warp & 3, sub = warp >> 2; // lanes 32*quarter.., columns 16*sub..
-            for (int mt = 0; mt < t.n_mt; mt++) {
-                const int row = mt * kTcRows + quarter * 32 + lane; // this thread's asset row
-                const uint32_t taddr = tmem + ((uint32_t)(quarter * 32) << 16) + (uint32_t)(mt * kTcPaths + sub * 16);
-                uint32_t v[16];
-                asm volatile("tcgen05.ld.sync.aligned.32x32b.x16.b32 "
-                             "{%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, [%16];"
-                             : "=r"(v[0]), "=r"(v[1]), "=r"(v[2]), "=r"(v[3]), "=r"(v[4]), "=r"(v[5]),
-                               "=r"(v[6]), "=r"(v[7]), "=r"(v[8]), "=r"(v[9]), "=r"(v[10]), "=r"(v[11]),
-                               "=r"(v[12]), "=r"(v[13]), "=r"(v[14]), "=r"(v[15])
-                             : "r"(taddr));
-                asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
-                // threshold on the scaled accumulator: D/2^8 < -x - H mu_i
-                const bool asset = row < n;
-                const float thr = asset ? (float)(((double)a.neg_x - (double)a.horizon * a.mu64[row]) * kTcLScale)
-                                        : 0.f;
-                int cnt = 0;
+                    if (lane < 16 && cnt) atomicAdd(&sS[sub * 16 + lane], cnt);
+                    if (row == n) {
 #pragma unroll
-                for (int c = 0; c < 16; c++) {
-                    const float d = __uint_as_float(v[c]);
-                    const unsigned m = __ballot_sync(0xffffffffu, asset && d < thr);
-                    if (lane == c) cnt = __popc(m);
-                }
-                if (lane < 16 && cnt) atomicAdd(&sS[sub * 16 + lane], cnt);
-                if (row == n) {
-#pragma unroll
-                    for (int c = 0; c < 16; c++)
-                        sPort[sub * 16 + c] = (float)(t.hwmu + (double)(__uint_as_float(v[c]) * (1.0f / kTcLScale)));
+                        for (int c = 0; c < 16; c++)
+                            sPort[sub * 16 + c] = (float)(it.hwmu + (double)(__uint_as_float(v[c]) * (1.0f / kTcLScale)));
+                    }
                 }
             }
-        }
-        tc_fence_before();
-        __syncthreads();
-        if (!s_abort && tid < kTcPaths) {
-            const long long p = p0 + tid;
-            if (p < a.n_paths) {
-                const int S = sS[tid];
-                const float port = sPort[tid];
-                crash += (S >= a.k) ? 1 : 0;
-                breach += (a.has_w && port < a.port_thr) ? 1 : 0;
-                if (a.s_values) a.s_values[p] = S;
-                if (a.port_values) a.port_values[p] = port;
-                if (VAR) var_path(a, port, nullptr, n_tail, tail_fx); // histogram pass: global atomics
+            tc_fence_before();
+            __syncthreads();
+            if (!s_abort && tid < kTcPaths) {
+                const long long p = p0 + tid;
+                const bool live = p < it.n_paths;
+                int crash = 0, breach = 0;
+                if (live) {
+                    const int S = sS[tid];
+                    const float port = sPort[tid];
+                    crash = (S >= it.k) ? 1 : 0;
+                    breach = (it.has_w && port < it.port_thr) ? 1 : 0;
+                    if (it.s_values) it.s_values[p] = S;
+                    if (it.port_values) it.port_values[p] = port;
+                    if (VAR) var_path(a, port, nullptr, n_tail, tail_fx); // histogram pass: global atomics
+                }
+                crash = __reduce_add_sync(0xffffffffu, crash);
+                breach = __reduce_add_sync(0xffffffffu, breach);
+                if (lane == 0) {
+                    if (crash) atomicAdd(&it.counts[0], (unsigned long long)crash);
+                    if (breach) atomicAdd(&it.counts[1], (unsigned long long)breach);
+                }
             }
+            __syncthreads();
+            tc_fence_after();
         }
-        __syncthreads();
-        tc_fence_after();
     }
 
     // ---- teardown: drain in-flight copies and MMAs (bounded), free TMEM
@@ -401,7 +445,7 @@ __global__ void __launch_bounds__(kTcThreads, 1) mc_tc_kernel(const TcArgs t)
     __syncthreads();
     tc_fence_after();
     if (warp == 0) asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(ncols));
-    cta_flush(a, crash, breach, n_tail, tail_fx, sacc, nullptr, VAR);
+    if (VAR) cta_flush(a, 0, 0, n_tail, tail_fx, sacc, nullptr, true);
 }
 
 // Pre-swizzled Lhat tiles: rows 0..N-1 = L (lower triangle), row N = w^T L,
@@ -443,8 +487,8 @@ __global__ void build_tc_tiles_kernel(const double *L, const float *w, int n, in
 }
 
 int tc_max_n() { return kTcMaxKt * kTcKt; }
-int tc_row_tiles(int n) { return (n + 1 + kTcRows - 1) / kTcRows; }
-int tc_k_tiles(int n) { return (n + kTcKt - 1) / kTcKt; }
+static int tc_row_tiles(int n) { return (n + 1 + kTcRows - 1) / kTcRows; }
+static int tc_k_tiles(int n) { return (n + kTcKt - 1) / kTcKt; }
 size_t tc_tile_bytes(int n) { return (size_t)tc_row_tiles(n) * tc_k_tiles(n) * 2 * kTcTileBytes; }
 
 cudaError_t launch_build_tc_tiles(const double *L64, const float *w32, int n, int bf16, unsigned char *tiles,
@@ -454,32 +498,124 @@ cudaError_t launch_build_tc_tiles(const double *L64, const float *w32, int n, in
     return cudaGetLastError();
 }
 
+static int tmem_cols_for(int n_mt)
+{
+    int c = 32;
+    while (c < n_mt * kTcPaths) c <<= 1;
+    return c;
+}
+
+static size_t tc_smem_bytes(int n_kt_max)
+{
+    return 1024 + (size_t)n_kt_max * 2 * kTcZBytes + (size_t)kTcStages * 2 * kTcTileBytes;
+}
+
+static void fill_item(TcItem &it, const PlainArgs &a, const unsigned char *tiles, int bf16, bool aggregated,
+                      double wmu, long long tile_begin)
+{
+    memset(&it, 0, sizeof(it));
+    it.tiles = tiles;
+    it.mu64 = a.mu64;
+    it.counts = a.counts;
+    it.s_values = a.s_values;
+    it.port_values = a.port_values;
+    it.path0 = a.path0;
+    it.n_paths = a.n_paths;
+    it.tile_begin = tile_begin;
+    it.keys = a.keys;
+    it.hwmu = (double)a.horizon * wmu;
+    it.n = a.n;
+    it.n_mt = tc_row_tiles(a.n);
+    it.n_kt = tc_k_tiles(a.n);
+    it.horizon = a.horizon;
+    it.k = a.k;
+    it.has_w = a.has_w;
+    it.aggregated = aggregated ? 1 : 0;
+    it.bf16 = bf16;
+    it.neg_x = a.neg_x;
+    it.port_thr = a.port_thr;
+    it.sqrt_h = sqrtf((float)a.horizon);
+}
+
 cudaError_t launch_tc(const PlainArgs &a, const unsigned char *tiles, int bf16, bool aggregated, double wmu,
                       unsigned int *err, bool inject_stall, int sm_count, cudaStream_t s)
 {
     if (a.n > tc_max_n()) return cudaErrorInvalidValue;
-    TcArgs t;
-    memset(&t, 0, sizeof(t));
-    t.a = a;
-    t.tiles = tiles;
-    t.n_mt = tc_row_tiles(a.n);
-    t.n_kt = tc_k_tiles(a.n);
-    t.bf16 = bf16;
-    t.aggregated = aggregated ? 1 : 0;
-    t.sqrt_h = sqrtf((float)a.horizon);
-    t.hwmu = (double)a.horizon * wmu;
-    t.err = err;
-    t.inject_stall = inject_stall ? 1 : 0;
-    if (t.n_mt * kTcPaths > 512) return cudaErrorInvalidValue;
-    const size_t smem = 1024 + (size_t)t.n_kt * 2 * kTcZBytes + (size_t)kTcStages * 2 * kTcTileBytes;
+    TcBatch b;
+    memset(&b, 0, sizeof(b));
+    fill_item(b.one, a, tiles, bf16, aggregated, wmu, 0);
+    b.items = nullptr;
+    b.n_items = 1;
+    b.unit_tiles = 1;
+    b.total_tiles = (a.n_paths + kTcPaths - 1) / kTcPaths;
+    b.work = nullptr;
+    b.err = err;
+    b.inject_stall = inject_stall ? 1 : 0;
+    b.n_kt_max = b.one.n_kt;
+    b.tmem_cols = tmem_cols_for(b.one.n_mt);
+    b.var = a;
+    if (b.one.n_mt * kTcPaths > 512) return cudaErrorInvalidValue;
+    const size_t smem = tc_smem_bytes(b.n_kt_max);
     auto kern = (a.var_mode != 0) ? mc_tc_kernel<true> : mc_tc_kernel<false>;
     cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess) return e;
-    long long tiles_n = (a.n_paths + kTcPaths - 1) / kTcPaths;
     long long grid = sm_count;
-    if (tiles_n < grid) grid = tiles_n;
-    kern<<<(unsigned)grid, kTcThreads, smem, s>>>(t);
+    if (b.total_tiles < grid) grid = b.total_tiles;
+    kern<<<(unsigned)grid, kTcThreads, smem, s>>>(b);
     return cudaGetLastError();
+}
+
+// Host-side description of one batch item for tc_batch_items.
+void tc_fill_batch_item(void *item_out, const PlainArgs &a, const unsigned char *tiles, int bf16,
+                        bool aggregated, double wmu, long long tile_begin)
+{
+    fill_item(*reinterpret_cast<TcItem *>(item_out), a, tiles, bf16, aggregated, wmu, tile_begin);
+}
+size_t tc_item_bytes() { return sizeof(TcItem); }
+long long tc_tiles_of(long long n_paths) { return (n_paths + kTcPaths - 1) / kTcPaths; }
+int tc_row_tiles_of(int n) { return tc_row_tiles(n); }
+int tc_k_tiles_of(int n) { return tc_k_tiles(n); }
+
+// One persistent launch over many items: CTAs claim units of `unit_tiles`
+// tiles from *work (zeroed by the caller).  tc_batch_prepare() must have
+// run (it is not a stream operation, so it stays out of graph captures).
+cudaError_t launch_tc_batch(const void *d_items, int n_items, long long total_tiles, int unit_tiles,
+                            unsigned int *work, unsigned int *err, int n_kt_max, int n_mt_max, int grid,
+                            cudaStream_t s)
+{
+    TcBatch b;
+    memset(&b, 0, sizeof(b));
+    b.items = reinterpret_cast<const TcItem *>(d_items);
+    b.n_items = n_items;
+    b.unit_tiles = unit_tiles < 1 ? 1 : unit_tiles;
+    b.total_tiles = total_tiles;
+    b.work = work;
+    b.err = err;
+    b.n_kt_max = n_kt_max;
+    b.tmem_cols = tmem_cols_for(n_mt_max);
+    if (n_mt_max * kTcPaths > 512 || n_kt_max > kTcMaxKt) return cudaErrorInvalidValue;
+    const size_t smem = tc_smem_bytes(n_kt_max);
+    mc_tc_kernel<false><<<(unsigned)grid, kTcThreads, smem, s>>>(b);
+    return cudaGetLastError();
+}
+
+// Resident CTAs per SM of the batched kernel for this largest item
+// (registers and shared memory; tensor memory is checked by the caller).
+int tc_batch_occupancy(int n_kt_max)
+{
+    int per_sm = 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, mc_tc_kernel<false>, kTcThreads,
+                                                      tc_smem_bytes(n_kt_max)) != cudaSuccess)
+        return 1;
+    return per_sm < 1 ? 1 : per_sm;
+}
+
+// Raise the kernel's dynamic shared-memory limit to the largest size a
+// batch can ask for; called once before any launch or capture.
+cudaError_t tc_batch_prepare()
+{
+    return cudaFuncSetAttribute(mc_tc_kernel<false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                (int)tc_smem_bytes(kTcMaxKt));
 }
 
 } // namespace rg

@@ -41,6 +41,8 @@ EXPORTED_SYMBOLS = [
     "rg_portfolio_create", "rg_portfolio_destroy", "rg_portfolio_info_get",
     "rg_portfolio_factor", "rg_simulate", "rg_launch_counts", "rg_run",
     "rg_estimator_stats", "rg_tail_count", "rg_probe_peaks", "rg_simulate_noalloc",
+    "rg_batch_create", "rg_batch_launch", "rg_batch_wait", "rg_batch_info_get", "rg_batch_tune",
+    "rg_batch_destroy",
     "get_cuda_model", "cuda_simulate",
 ]
 
@@ -115,6 +117,16 @@ class ModelFunctions(ctypes.Structure):
     _fields_ = [("name", ctypes.c_char_p), ("run_model", ModelRunFunc)]
 
 
+class BatchItem(ctypes.Structure):
+    _fields_ = [("portfolio", ctypes.c_void_p), ("query", Query)]
+
+
+class BatchInfo(ctypes.Structure):
+    _fields_ = [("items", ctypes.c_int32), ("total_tiles", ctypes.c_int64), ("unit_tiles", ctypes.c_int32),
+                ("ctas_per_sm", ctypes.c_int32), ("grid", ctypes.c_int32), ("graph", ctypes.c_int32),
+                ("tuned", ctypes.c_int32), ("last_ms", ctypes.c_float)]
+
+
 class Peaks(ctypes.Structure):
     _fields_ = [("fp32_tflops", ctypes.c_double), ("normals_per_s", ctypes.c_double),
                 ("sm_count", ctypes.c_int32)]
@@ -150,6 +162,13 @@ def lib():
         L.rg_estimator_stats.restype = None
         L.rg_tail_count.argtypes = [ctypes.c_int64, ctypes.c_double]
         L.rg_tail_count.restype = ctypes.c_int64
+        L.rg_batch_create.argtypes = [ctypes.POINTER(BatchItem), ctypes.c_int32, ctypes.c_int32,
+                                      ctypes.POINTER(ctypes.c_void_p)]
+        L.rg_batch_launch.argtypes = [ctypes.c_void_p, ctypes.c_void_p]
+        L.rg_batch_wait.argtypes = [ctypes.c_void_p, ctypes.POINTER(Result)]
+        L.rg_batch_info_get.argtypes = [ctypes.c_void_p, ctypes.POINTER(BatchInfo)]
+        L.rg_batch_tune.argtypes = [ctypes.c_void_p, ctypes.c_void_p]
+        L.rg_batch_destroy.argtypes = [ctypes.c_void_p]
         L.rg_probe_peaks.argtypes = [ctypes.POINTER(Peaks), ctypes.c_void_p]
         L.get_cuda_model.restype = ModelFunctions
         L.cuda_simulate.argtypes = [ctypes.POINTER(MonteCarloParams), ctypes.POINTER(MonteCarloResult)]
@@ -220,6 +239,55 @@ class Portfolio:
     def close(self):
         if self._h:
             lib().rg_portfolio_destroy(self._h)
+            self._h = ctypes.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+BATCH_NO_GRAPH = 0x1
+
+
+class Batch:
+    """Many (Portfolio, Query) items in one persistent tensor-core launch,
+    replayed from a captured CUDA graph (rg_batch_*)."""
+
+    def __init__(self, items, flags=0):
+        self._ports = [p for p, _ in items]  # keep the portfolios alive
+        arr = (BatchItem * len(items))()
+        for i, (p, q) in enumerate(items):
+            arr[i].portfolio = p.handle
+            arr[i].query = q
+        self.count = len(items)
+        self._h = ctypes.c_void_p()
+        check(lib().rg_batch_create(arr, self.count, flags, ctypes.byref(self._h)))
+
+    def launch(self, stream=None):
+        check(lib().rg_batch_launch(self._h, stream))
+
+    def wait(self):
+        res = (Result * self.count)()
+        check(lib().rg_batch_wait(self._h, res))
+        return [r.as_dict() for r in res]
+
+    def run(self, stream=None):
+        self.launch(stream)
+        return self.wait()
+
+    def tune(self, stream=None):
+        check(lib().rg_batch_tune(self._h, stream))
+
+    def info(self):
+        inf = BatchInfo()
+        check(lib().rg_batch_info_get(self._h, ctypes.byref(inf)))
+        return {f: getattr(inf, f) for f, _ in inf._fields_}
+
+    def close(self):
+        if self._h:
+            lib().rg_batch_destroy(self._h)
             self._h = ctypes.c_void_p()
 
     def __del__(self):

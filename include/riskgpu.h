@@ -156,6 +156,43 @@ void rg_estimator_stats(int64_t count, int64_t M, double *p, double *se, double 
 /* VaR tail size used by the engine: ceil((1-level) M), clamped to [1, M]. */
 int64_t rg_tail_count(int64_t M, double level);
 
+/* ---------------- batches: many queries, one persistent launch ---------------- */
+/* No counterpart in the reference (one model run per call,
+ * src/main_runner.c:198-298).  A batch holds up to thousands of
+ * (portfolio, query) items of uneven N, H and path counts; one launch of
+ * the persistent tensor-core kernel computes all of them, CTAs claiming
+ * work units of 64-path tiles from a device counter.  The launch (counter
+ * resets, kernel, copy of the counts to pinned host memory) is captured
+ * once into a CUDA graph and replayed by rg_batch_launch.  Items use the
+ * Philox layout, N <= 640, precision FP16X3 (BF16X3 if asked), no VaR. */
+typedef struct rg_batch rg_batch;
+typedef struct {
+    const rg_portfolio *portfolio;
+    rg_query query;
+} rg_batch_item;
+typedef struct {
+    int32_t items;
+    int64_t total_tiles;   /* 64-path tiles over all items */
+    int32_t unit_tiles;    /* tiles per work unit */
+    int32_t ctas_per_sm;
+    int32_t grid;
+    int32_t graph;         /* 1 = replayed from a captured CUDA graph */
+    int32_t tuned;         /* 1 = parameters from the autotuner */
+    float last_ms;         /* device time of the last launch */
+} rg_batch_info;
+#define RG_BATCH_NO_GRAPH 0x1 /* launch without graph capture */
+int rg_batch_create(const rg_batch_item *items, int32_t count, int32_t flags, rg_batch **out);
+int rg_batch_launch(rg_batch *b, void *stream);
+/* Waits for the last launch and fills results[count] (no VaR fields). */
+int rg_batch_wait(rg_batch *b, rg_result *results);
+int rg_batch_info_get(const rg_batch *b, rg_batch_info *out);
+/* Autotuner: times every (tiles per unit, CTAs per SM) candidate for this
+ * batch's shape class, keeps the fastest for this batch and records it in
+ * the JSON cache (RG_TUNE_CACHE, default ./riskgpu_tune.json) that later
+ * batches of the class read at creation. */
+int rg_batch_tune(rg_batch *b, void *stream);
+int rg_batch_destroy(rg_batch *b);
+
 /* ---------------- simulation without allocation ---------------- */
 /* No counterpart in the reference.  rg_simulate() with no allocation at all,
  * for callers that cannot call cudaMalloc where they run a query: a host

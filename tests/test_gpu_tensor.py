@@ -106,3 +106,62 @@ def test_tc_statistics_vs_fp32_and_closed_form(gpu, oracle):
         r = port.simulate(gpu.make_query(M, 21, x=p.x, k=p.k, horizon=p.horizon,
                                          port_threshold=p.port_threshold, precision=prec))
         assert abs(r["p_breach"] - cf["p_breach"]) < 3 * se, (prec, r["p_breach"], cf["p_breach"])
+
+
+# ------------------------------------------------------------------ batches
+def _batch_items(gpu, count, seed=4096, m_range=(2e3, 6e4), n_max=600):
+    from riskgpu import synth
+    ps = synth.batch_256(count=count, base_seed=seed, n_max=n_max, m_range=m_range)
+    items = []
+    for p in ps:
+        port = gpu.Portfolio(p.mu, p.sigma, p.weights)
+        q = gpu.make_query(p.n_paths, p.seed, x=p.x, k=p.k, horizon=p.horizon,
+                           port_threshold=p.port_threshold, precision=3)
+        items.append((port, q))
+    return ps, items
+
+
+@pytest.mark.parametrize("flags", [0, 1])
+def test_batch_equals_individual_queries(gpu, flags):
+    """Each item's counts from one persistent batched launch equal the counts
+    of the same query run alone (same per-path arithmetic, integer counts):
+    results do not depend on batching.  With and without the CUDA graph;
+    two launches of the same batch agree."""
+    ps, items = _batch_items(gpu, 24)
+    batch = gpu.Batch(items, flags=flags)
+    res = batch.run()
+    res2 = batch.run()
+    for (port, q), r, r2 in zip(items, res, res2):
+        alone = port.simulate(q)
+        assert (r["crash_count"], r["breach_count"]) == (alone["crash_count"], alone["breach_count"])
+        assert (r2["crash_count"], r2["breach_count"]) == (r["crash_count"], r["breach_count"])
+    inf = batch.info()
+    assert inf["graph"] == (0 if flags else 1) and inf["items"] == 24
+
+
+def test_batch_autotuner_persists_choice(gpu, tmp_path, monkeypatch):
+    monkeypatch.setenv("RG_TUNE_CACHE", str(tmp_path / "tune.json"))
+    ps, items = _batch_items(gpu, 12, seed=7)
+    b = gpu.Batch(items)
+    before = b.run()
+    b.tune()
+    after = b.run()
+    assert [(r["crash_count"], r["breach_count"]) for r in before] == \
+           [(r["crash_count"], r["breach_count"]) for r in after]
+    inf = b.info()
+    assert inf["tuned"] == 1
+    import json
+    cache = json.load(open(tmp_path / "tune.json"))
+    assert len(cache) == 1 and list(cache.values())[0][:2] == [inf["unit_tiles"], inf["ctas_per_sm"]]
+    b2 = gpu.Batch(items)
+    assert b2.info()["tuned"] == 1 and b2.info()["unit_tiles"] == inf["unit_tiles"]
+
+
+def test_batch_rejects_unsupported_items(gpu):
+    from riskgpu import synth
+    p = synth.one_factor_20(n_paths=1)
+    port = gpu.Portfolio(p.mu, p.sigma, p.weights)
+    with pytest.raises(gpu.RiskGpuError):
+        gpu.Batch([(port, gpu.make_query(1000, 1, var_level=0.99, precision=3))])
+    with pytest.raises(gpu.RiskGpuError):
+        gpu.Batch([(port, gpu.make_query(1000, 1, rng=gpu.RNG_XORWOW_REF))])
