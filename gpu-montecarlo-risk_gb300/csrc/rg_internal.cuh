@@ -197,7 +197,8 @@ int tc_row_tiles_of(int n);
 int tc_k_tiles_of(int n);
 cudaError_t launch_tc_batch(const void *d_items, int n_items, long long total_tiles, int unit_tiles,
                             unsigned int *work, unsigned int *err, int n_kt_max, int n_mt_max, int grid,
-                            cudaStream_t s);
+                            cudaStream_t s, const long long *dyn = nullptr);
+int tc_max_k_tiles();
 cudaError_t tc_batch_prepare();
 int tc_batch_occupancy(int n_kt_max);
 // rg_mc_fused.cu: N <= 64 kernel, L in parameter space; Philox only.

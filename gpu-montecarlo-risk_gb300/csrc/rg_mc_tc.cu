@@ -83,6 +83,8 @@ struct TcBatch {
     int inject_stall;         // host-side fault injection: one stage is never filled
     int n_kt_max;             // K tiles of the largest item (shared-memory size)
     int tmem_cols;            // tensor-memory columns allocated (power of 2 >= 64 n_mt_max)
+    const long long *dyn;     // if set: [0] items, [1] total tiles, read from device memory
+                              // (a graph captured once serves batches of any size)
     PlainArgs var;            // VaR fields of a single-item query (var_mode 0 otherwise)
 };
 
@@ -243,7 +245,8 @@ __global__ void __launch_bounds__(kTcThreads, 1) mc_tc_kernel(const __grid_const
     long long tail_fx = 0;
     // pipeline state (kept across tiles)
     unsigned prod_iter = 0, cons_iter = 0, tile_iter = 0;
-    const long long total = b.total_tiles;
+    const long long total = b.dyn ? b.dyn[1] : b.total_tiles;
+    const int n_items = b.dyn ? (int)b.dyn[0] : b.n_items;
 
     for (long long round = 0;; round++) {
         // claim a work unit: dynamic (atomic counter) for batches, static otherwise
@@ -256,7 +259,7 @@ __global__ void __launch_bounds__(kTcThreads, 1) mc_tc_kernel(const __grid_const
         for (long long tile = unit * b.unit_tiles; tile < tend; tile++, tile_iter++) {
             if (s_abort) break;
             // the item of this tile (items are ordered by tile_begin)
-            int lo = 0, hi = b.n_items - 1;
+            int lo = 0, hi = n_items - 1;
             const TcItem *items = b.items ? b.items : &b.one;
             while (lo < hi) {
                 const int mid = (lo + hi + 1) >> 1;
@@ -487,6 +490,7 @@ __global__ void build_tc_tiles_kernel(const double *L, const float *w, int n, in
 }
 
 int tc_max_n() { return kTcMaxKt * kTcKt; }
+int tc_max_k_tiles() { return kTcMaxKt; }
 static int tc_row_tiles(int n) { return (n + 1 + kTcRows - 1) / kTcRows; }
 static int tc_k_tiles(int n) { return (n + kTcKt - 1) / kTcKt; }
 size_t tc_tile_bytes(int n) { return (size_t)tc_row_tiles(n) * tc_k_tiles(n) * 2 * kTcTileBytes; }
@@ -581,10 +585,11 @@ int tc_k_tiles_of(int n) { return tc_k_tiles(n); }
 // run (it is not a stream operation, so it stays out of graph captures).
 cudaError_t launch_tc_batch(const void *d_items, int n_items, long long total_tiles, int unit_tiles,
                             unsigned int *work, unsigned int *err, int n_kt_max, int n_mt_max, int grid,
-                            cudaStream_t s)
+                            cudaStream_t s, const long long *dyn)
 {
     TcBatch b;
     memset(&b, 0, sizeof(b));
+    b.dyn = dyn;
     b.items = reinterpret_cast<const TcItem *>(d_items);
     b.n_items = n_items;
     b.unit_tiles = unit_tiles < 1 ? 1 : unit_tiles;

@@ -42,7 +42,9 @@ EXPORTED_SYMBOLS = [
     "rg_portfolio_factor", "rg_simulate", "rg_launch_counts", "rg_run",
     "rg_estimator_stats", "rg_tail_count", "rg_probe_peaks", "rg_simulate_noalloc",
     "rg_batch_create", "rg_batch_launch", "rg_batch_wait", "rg_batch_info_get", "rg_batch_tune",
-    "rg_batch_destroy",
+    "rg_batch_destroy", "rg_server_default_config", "rg_server_create", "rg_server_register",
+    "rg_server_submit", "rg_server_wait", "rg_server_stats", "rg_server_reset_stats",
+    "rg_server_destroy",
     "get_cuda_model", "cuda_simulate",
 ]
 
@@ -127,6 +129,18 @@ class BatchInfo(ctypes.Structure):
                 ("tuned", ctypes.c_int32), ("last_ms", ctypes.c_float)]
 
 
+class ServerConfig(ctypes.Structure):
+    _fields_ = [("slots", ctypes.c_int32), ("max_batch_items", ctypes.c_int32),
+                ("headroom_bytes", ctypes.c_int64), ("admission_timeout_ms", ctypes.c_double),
+                ("poll_us", ctypes.c_int32)]
+
+
+class ServerStats(ctypes.Structure):
+    _fields_ = [("completed", ctypes.c_int64), ("refused", ctypes.c_int64), ("batches", ctypes.c_int64),
+                ("mean_batch_items", ctypes.c_double), ("p50_ms", ctypes.c_double),
+                ("p99_ms", ctypes.c_double), ("max_ms", ctypes.c_double), ("paths_per_s", ctypes.c_double)]
+
+
 class Peaks(ctypes.Structure):
     _fields_ = [("fp32_tflops", ctypes.c_double), ("normals_per_s", ctypes.c_double),
                 ("sm_count", ctypes.c_int32)]
@@ -169,6 +183,17 @@ def lib():
         L.rg_batch_info_get.argtypes = [ctypes.c_void_p, ctypes.POINTER(BatchInfo)]
         L.rg_batch_tune.argtypes = [ctypes.c_void_p, ctypes.c_void_p]
         L.rg_batch_destroy.argtypes = [ctypes.c_void_p]
+        L.rg_server_default_config.argtypes = [ctypes.POINTER(ServerConfig)]
+        L.rg_server_default_config.restype = None
+        L.rg_server_create.argtypes = [ctypes.POINTER(ServerConfig), ctypes.POINTER(ctypes.c_void_p)]
+        L.rg_server_register.argtypes = [ctypes.c_void_p, ctypes.c_int32, ctypes.c_void_p]
+        L.rg_server_submit.argtypes = [ctypes.c_void_p, ctypes.c_int32, ctypes.POINTER(Query),
+                                       ctypes.POINTER(ctypes.c_uint64)]
+        L.rg_server_wait.argtypes = [ctypes.c_void_p, ctypes.c_uint64, ctypes.POINTER(Result),
+                                     ctypes.POINTER(ctypes.c_double)]
+        L.rg_server_stats.argtypes = [ctypes.c_void_p, ctypes.POINTER(ServerStats)]
+        L.rg_server_reset_stats.argtypes = [ctypes.c_void_p]
+        L.rg_server_destroy.argtypes = [ctypes.c_void_p]
         L.rg_probe_peaks.argtypes = [ctypes.POINTER(Peaks), ctypes.c_void_p]
         L.get_cuda_model.restype = ModelFunctions
         L.cuda_simulate.argtypes = [ctypes.POINTER(MonteCarloParams), ctypes.POINTER(MonteCarloResult)]
@@ -288,6 +313,64 @@ class Batch:
     def close(self):
         if self._h:
             lib().rg_batch_destroy(self._h)
+            self._h = ctypes.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+class Server:
+    """Request loop with continuous batching (rg_server_*)."""
+
+    def __init__(self, **cfg):
+        c = ServerConfig()
+        lib().rg_server_default_config(ctypes.byref(c))
+        for k, v in cfg.items():
+            setattr(c, k, v)
+        self._h = ctypes.c_void_p()
+        self._ports = {}
+        check(lib().rg_server_create(ctypes.byref(c), ctypes.byref(self._h)))
+
+    def register(self, pid, portfolio):
+        self._ports[pid] = portfolio
+        check(lib().rg_server_register(self._h, int(pid), portfolio.handle))
+
+    def submit(self, pid, query) -> int:
+        t = ctypes.c_uint64()
+        check(lib().rg_server_submit(self._h, int(pid), ctypes.byref(query), ctypes.byref(t)))
+        return t.value
+
+    def wait(self, ticket):
+        r = Result()
+        lat = ctypes.c_double()
+        check(lib().rg_server_wait(self._h, ticket, ctypes.byref(r), ctypes.byref(lat)))
+        d = r.as_dict()
+        d["latency_ms"] = lat.value
+        return d
+
+    def try_wait(self, ticket):
+        """(status, result) without raising."""
+        r = Result()
+        lat = ctypes.c_double()
+        st = lib().rg_server_wait(self._h, ticket, ctypes.byref(r), ctypes.byref(lat))
+        d = r.as_dict()
+        d["latency_ms"] = lat.value
+        return st, d
+
+    def stats(self):
+        s = ServerStats()
+        check(lib().rg_server_stats(self._h, ctypes.byref(s)))
+        return {f: getattr(s, f) for f, _ in s._fields_}
+
+    def reset_stats(self):
+        check(lib().rg_server_reset_stats(self._h))
+
+    def close(self):
+        if self._h:
+            lib().rg_server_destroy(self._h)
             self._h = ctypes.c_void_p()
 
     def __del__(self):

@@ -193,6 +193,42 @@ int rg_batch_info_get(const rg_batch *b, rg_batch_info *out);
 int rg_batch_tune(rg_batch *b, void *stream);
 int rg_batch_destroy(rg_batch *b);
 
+/* ---------------- served form: request loop with continuous batching ---------------- */
+/* No counterpart in the reference.  A server keeps registered portfolios
+ * resident and runs a scheduler thread: requests that arrive are admitted
+ * while free HBM (cudaMemGetInfo) stays above headroom_bytes, packed into
+ * one of `slots` preallocated, graph-captured persistent batches (up to
+ * max_batch_items requests each) and launched while earlier batches may
+ * still be running; completions are polled every poll_us.  A request's
+ * result does not depend on the batch that carried it (draws are keyed by
+ * seed and path index).  Requests use the Philox layout, N <= 640, no VaR;
+ * the portfolios stay owned by the caller and must outlive the server. */
+typedef struct rg_server rg_server;
+typedef struct {
+    int32_t slots;               /* batches in flight on the GPU (default 3) */
+    int32_t max_batch_items;     /* requests per batch (default 64) */
+    int64_t headroom_bytes;      /* admission: free HBM must exceed this (default 1 GiB) */
+    double admission_timeout_ms; /* pending longer than this without headroom: RG_ERR_ADMISSION */
+    int32_t poll_us;             /* completion polling interval while work is in flight */
+} rg_server_config;
+typedef struct {
+    int64_t completed;
+    int64_t refused;
+    int64_t batches;
+    double mean_batch_items;
+    double p50_ms, p99_ms, max_ms; /* submit-to-result latency of completed requests */
+    double paths_per_s;            /* paths completed / (last completion - first submit) */
+} rg_server_summary;
+void rg_server_default_config(rg_server_config *cfg);
+int rg_server_create(const rg_server_config *cfg, rg_server **out);
+int rg_server_register(rg_server *s, int32_t portfolio_id, const rg_portfolio *p);
+int rg_server_submit(rg_server *s, int32_t portfolio_id, const rg_query *q, uint64_t *ticket);
+/* Blocks until the request is done; latency_ms (nullable) = submit to result. */
+int rg_server_wait(rg_server *s, uint64_t ticket, rg_result *out, double *latency_ms);
+int rg_server_stats(rg_server *s, rg_server_summary *out);
+int rg_server_reset_stats(rg_server *s);
+int rg_server_destroy(rg_server *s);
+
 /* ---------------- simulation without allocation ---------------- */
 /* No counterpart in the reference.  rg_simulate() with no allocation at all,
  * for callers that cannot call cudaMalloc where they run a query: a host

@@ -165,3 +165,56 @@ def test_batch_rejects_unsupported_items(gpu):
         gpu.Batch([(port, gpu.make_query(1000, 1, var_level=0.99, precision=3))])
     with pytest.raises(gpu.RiskGpuError):
         gpu.Batch([(port, gpu.make_query(1000, 1, rng=gpu.RNG_XORWOW_REF))])
+
+
+# ------------------------------------------------------------------ serving
+def test_server_results_equal_alone_and_in_the_mix(gpu):
+    """Continuous batching: many requests from several client threads,
+    arriving while others run; every result equals the same query run
+    alone (integer counts, exactly)."""
+    import threading
+    ps, items = _batch_items(gpu, 16, seed=99, m_range=(1e3, 2e4))
+    srv = gpu.Server(slots=3, max_batch_items=8, poll_us=20)
+    for i, (port, _) in enumerate(items):
+        srv.register(i, port)
+    results = {}
+
+    def client(ids):
+        for rep in range(3):
+            for i in ids:
+                tk = srv.submit(i, items[i][1])
+                results[(i, rep, threading.get_ident())] = srv.wait(tk)
+
+    th = [threading.Thread(target=client, args=(list(range(j, 16, 4)),)) for j in range(4)]
+    for t in th:
+        t.start()
+    for t in th:
+        t.join()
+    alone = [port.simulate(q) for port, q in items]
+    assert len(results) == 16 * 3
+    for (i, rep, _), r in results.items():
+        assert (r["crash_count"], r["breach_count"]) == (alone[i]["crash_count"], alone[i]["breach_count"])
+        assert r["latency_ms"] > 0
+    st = srv.stats()
+    assert st["completed"] == 48 and st["p99_ms"] >= st["p50_ms"] > 0
+    assert st["batches"] >= 1
+    srv.close()
+
+
+def test_server_admission_by_headroom(gpu):
+    """With a headroom larger than the device, requests are never admitted and
+    fail with RG_ERR_ADMISSION after the admission timeout; a server with a
+    normal headroom serves the same request."""
+    ps, items = _batch_items(gpu, 1, seed=5, m_range=(1e3, 2e3))
+    port, q = items[0]
+    srv = gpu.Server(headroom_bytes=1 << 60, admission_timeout_ms=200.0)
+    srv.register(0, port)
+    st, _ = srv.try_wait(srv.submit(0, q))
+    assert st == gpu.RG_ERR_ADMISSION
+    assert srv.stats()["refused"] == 1
+    srv.close()
+    srv = gpu.Server()
+    srv.register(0, port)
+    r = srv.wait(srv.submit(0, q))
+    assert r["crash_count"] == port.simulate(q)["crash_count"]
+    srv.close()
