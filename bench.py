@@ -63,7 +63,7 @@ def parse():
                     help="approximate CPU time of the bounded CPU samples")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--workload", default="one_factor_50",
-                    choices=["one_factor_50", "five_factor_600"],
+                    choices=["one_factor_50", "five_factor_600", "batch_256", "served"],
                     help="one_factor_50 is the headline; five_factor_600 (N=600, H=10, "
                          "M=1e7 per step) is the precision-form workload")
     ap.add_argument("--draw-mode", default="daily", choices=["daily", "aggregated"])
@@ -376,10 +376,144 @@ def engine_arm(args):
         dist.destroy_process_group()
 
 
+def batch_arm(args):
+    """256 portfolios (N ~ U{10..600}, H ~ U{1..20}, M log-uniform [1e4, 1e6],
+    3-factor covariance, per-portfolio seed, thresholds U(-5%, -1%)) in one
+    persistent tensor-core launch replayed from a CUDA graph, against
+    per-portfolio launches of the plain FP32 kernels and of the tensor-core
+    kernel."""
+    import torch
+    import riskgpu
+    from riskgpu import synth
+    torch.cuda.set_device(0)
+    ps = synth.batch_256()
+    ports = [riskgpu.Portfolio(p.mu, p.sigma, p.weights) for p in ps]
+
+    def q(p, prec):
+        return riskgpu.make_query(p.n_paths, p.seed, x=p.x, k=p.k, horizon=p.horizon,
+                                  port_threshold=p.port_threshold, precision=prec)
+    total = sum(p.n_paths for p in ps)
+    batch = riskgpu.Batch([(pt, q(p, riskgpu.PREC_FP16X3)) for pt, p in zip(ports, ps)])
+    batch.run()
+    batch.tune()
+    for _ in range(args.warmup):
+        batch.run()
+    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
+    stream = torch.cuda.Stream()
+    clocks = ClockSampler(0)
+    clocks.start()
+    torch.cuda.synchronize()
+    for i in range(args.steps):
+        ev[i][0].record(stream)
+        batch.launch(stream.cuda_stream)
+        ev[i][1].record(stream)
+    res = batch.wait()
+    torch.cuda.synchronize()
+    clk = clocks.stop()
+    ms = sum(a.elapsed_time(b) for a, b in ev) / args.steps
+    value = total / (ms * 1e-3)
+    # per-portfolio launches, device-timed, same queries
+    def per_item(prec):
+        t0 = time.perf_counter()
+        dev = 0.0
+        for pt, p in zip(ports, ps):
+            dev += pt.simulate(q(p, prec))["ms_device"]
+        return total / (time.perf_counter() - t0), total / (dev * 1e-3)
+    plain_wall, plain_dev = per_item(riskgpu.PREC_FP32)
+    tc_wall, tc_dev = per_item(riskgpu.PREC_FP16X3)
+    same = all(r["crash_count"] == pt.simulate(q(p, riskgpu.PREC_FP16X3))["crash_count"]
+               for r, pt, p in list(zip(res, ports, ps))[:16])
+    line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": 1, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f16x3", "data": "synthetic",
+            "config": {"workload": "batch_256", "portfolios": len(ps), "paths_per_step": total,
+                       "n_assets": "U{10..600}", "horizon_days": "U{1..20}",
+                       "paths": "log-uniform [1e4, 1e6]", "launch": "one persistent tcgen05 launch, CUDA graph",
+                       "batch": batch.info()},
+            "per_portfolio_launches": {"plain_fp32_paths_per_s_wall": plain_wall,
+                                       "plain_fp32_paths_per_s_device": plain_dev,
+                                       "tensor_paths_per_s_wall": tc_wall,
+                                       "tensor_paths_per_s_device": tc_dev,
+                                       "batched_over_plain_device": value / plain_dev},
+            "results_equal_alone_first16": same, "clocks": clk, "gpu_launches": args.steps}
+    print(json.dumps(line), flush=True)
+
+
+def served_arm(args):
+    """Poisson arrivals at 2000 queries/s, each a 64-recurring-portfolio
+    query drawn as in batch_256 with M = 1e5, through the server (continuous
+    batching); against per-query launches of the plain FP32 kernel."""
+    import torch
+    import numpy as np
+    import riskgpu
+    from riskgpu import synth
+    torch.cuda.set_device(0)
+    ps = synth.batch_256(count=64, base_seed=5150)
+    ports = [riskgpu.Portfolio(p.mu, p.sigma, p.weights) for p in ps]
+    rng = np.random.default_rng(2000)
+    rate, seconds = 2000.0, max(1.0, float(args.steps) / 10.0)
+    nq = int(rate * seconds)
+    picks = rng.integers(0, 64, nq)
+    gaps = rng.exponential(1.0 / rate, nq)
+    queries = [riskgpu.make_query(100_000, int(ps[i].seed) + j, x=ps[i].x, k=ps[i].k, horizon=ps[i].horizon,
+                                  port_threshold=ps[i].port_threshold, precision=riskgpu.PREC_FP16X3)
+               for j, i in enumerate(picks)]
+    srv = riskgpu.Server(slots=3, max_batch_items=64, poll_us=20)
+    for i, pt in enumerate(ports):
+        srv.register(i, pt)
+    # warm-up
+    for t in [srv.submit(int(picks[j]), queries[j]) for j in range(64)]:
+        srv.wait(t)
+    srv.reset_stats()
+    clocks = ClockSampler(0)
+    clocks.start()
+    t0 = time.perf_counter()
+    tickets = []
+    next_t = t0
+    for j in range(nq):
+        next_t += gaps[j]
+        while time.perf_counter() < next_t:
+            pass
+        tickets.append(srv.submit(int(picks[j]), queries[j]))
+    for t in tickets:
+        srv.wait(t)
+    wall = time.perf_counter() - t0
+    clk = clocks.stop()
+    st = srv.stats()
+    srv.close()
+    # per-query launches of the plain kernel, one at a time
+    lat = []
+    t1 = time.perf_counter()
+    for j in range(min(nq, 400)):
+        s = time.perf_counter()
+        qq = queries[j]
+        qq.precision = riskgpu.PREC_FP32
+        ports[picks[j]].simulate(qq)
+        lat.append(1e3 * (time.perf_counter() - s))
+    plain_s = time.perf_counter() - t1
+    lat.sort()
+    line = {"metric": "served_paths_per_second", "value": st["paths_per_s"], "unit": UNIT, "n_gpus": 1,
+            "steps": nq, "warmup": 64, "ms_per_step": 1e3 * wall / nq, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f16x3", "data": "synthetic",
+            "config": {"workload": "served", "arrivals": "Poisson 2000/s", "queries": nq,
+                       "paths_per_query": 100_000, "portfolios": 64, "offered_paths_per_s": rate * 1e5},
+            "latency_ms": {"p50": st["p50_ms"], "p99": st["p99_ms"], "max": st["max_ms"]},
+            "server": st, "wall_s": wall,
+            "per_query_plain": {"queries": len(lat), "queries_per_s": len(lat) / plain_s,
+                                "paths_per_s": len(lat) * 1e5 / plain_s,
+                                "service_p50_ms": lat[len(lat) // 2], "service_p99_ms": lat[int(0.99 * len(lat)) - 1]},
+            "clocks": clk}
+    print(json.dumps(line), flush=True)
+
+
 def main():
     args = parse()
     if args.impl == "reference":
         reference_arm(args)
+    elif args.workload == "batch_256":
+        batch_arm(args)
+    elif args.workload == "served":
+        served_arm(args)
     else:
         engine_arm(args)
 
