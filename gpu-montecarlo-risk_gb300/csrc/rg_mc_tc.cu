@@ -197,7 +197,10 @@ __device__ __forceinline__ void split2(float v, int bf16, unsigned short &hi, un
     }
 }
 
-template <bool VAR>
+// BATCH = false: one query, its item read straight from the kernel's
+// parameter space (constant-bank operands in the generator); BATCH = true:
+// the item table in device memory, the current item staged in shared memory.
+template <bool VAR, bool BATCH>
 __global__ void __launch_bounds__(kTcThreads, 1) mc_tc_kernel(const __grid_constant__ TcBatch b)
 {
     extern __shared__ __align__(1024) unsigned char tc_smem[];
@@ -216,6 +219,8 @@ __global__ void __launch_bounds__(kTcThreads, 1) mc_tc_kernel(const __grid_const
     __shared__ unsigned s_cons; // stages the MMA thread has consumed (for the abort drain)
     __shared__ long long s_unit;
     __shared__ unsigned long long sacc[4];
+    __shared__ __align__(16) TcItem s_item; // BATCH: the current item
+    int cur_item = -1;
 
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
     const int ncols = b.tmem_cols;
@@ -259,13 +264,21 @@ __global__ void __launch_bounds__(kTcThreads, 1) mc_tc_kernel(const __grid_const
         for (long long tile = unit * b.unit_tiles; tile < tend; tile++, tile_iter++) {
             if (s_abort) break;
             // the item of this tile (items are ordered by tile_begin)
-            int lo = 0, hi = n_items - 1;
-            const TcItem *items = b.items ? b.items : &b.one;
-            while (lo < hi) {
-                const int mid = (lo + hi + 1) >> 1;
-                if (items[mid].tile_begin <= tile) lo = mid; else hi = mid - 1;
+            if (BATCH) {
+                int lo = 0, hi = n_items - 1;
+                while (lo < hi) {
+                    const int mid = (lo + hi + 1) >> 1;
+                    if (b.items[mid].tile_begin <= tile) lo = mid; else hi = mid - 1;
+                }
+                if (lo != cur_item) { // uniform: every thread computed the same index
+                    const int *src = reinterpret_cast<const int *>(&b.items[lo]);
+                    int *dst = reinterpret_cast<int *>(&s_item);
+                    for (int w = tid; w < (int)(sizeof(TcItem) / 4); w += blockDim.x) dst[w] = src[w];
+                    cur_item = lo;
+                    __syncthreads();
+                }
             }
-            const TcItem &it = items[lo];
+            const TcItem &it = BATCH ? s_item : b.one;
             const int n = it.n, nq = (n + 3) >> 2, n_kt = it.n_kt, n_mt = it.n_mt;
             const long long p0 = (tile - it.tile_begin) * kTcPaths; // first path of the tile (item-local)
             // ---- 1. normals -> swizzled hi/lo Z tiles
@@ -374,17 +387,27 @@ __global__ void __launch_bounds__(kTcThreads, 1) mc_tc_kernel(const __grid_const
             }
             tc_fence_after();
             if (done_ok && !s_abort) {
-                const int quarter = warp & 3, sub = warp >> 2; // lanes 32*quarter.., columns 16*sub..
+                constexpr int kGroups = kTcThreads / 128;          // column groups
+                constexpr int kCols = kTcPaths / kGroups;          // columns per warp
+                const int quarter = warp & 3, sub = warp >> 2;     // lanes 32*quarter.., columns kCols*sub..
                 for (int mt = 0; mt < n_mt; mt++) {
                     const int row = mt * kTcRows + quarter * 32 + lane; // this thread's asset row
-                    const uint32_t taddr = tmem + ((uint32_t)(quarter * 32) << 16) + (uint32_t)(mt * kTcPaths + sub * 16);
-                    uint32_t v[16];
-                    asm volatile("tcgen05.ld.sync.aligned.32x32b.x16.b32 "
-                                 "{%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, [%16];"
-                                 : "=r"(v[0]), "=r"(v[1]), "=r"(v[2]), "=r"(v[3]), "=r"(v[4]), "=r"(v[5]),
-                                   "=r"(v[6]), "=r"(v[7]), "=r"(v[8]), "=r"(v[9]), "=r"(v[10]), "=r"(v[11]),
-                                   "=r"(v[12]), "=r"(v[13]), "=r"(v[14]), "=r"(v[15])
-                                 : "r"(taddr));
+                    const uint32_t taddr = tmem + ((uint32_t)(quarter * 32) << 16) + (uint32_t)(mt * kTcPaths + sub * kCols);
+                    uint32_t v[kCols];
+                    static_assert(kCols == 8 || kCols == 16, "epilogue load shape");
+                    if constexpr (kCols == 16) {
+                        asm volatile("tcgen05.ld.sync.aligned.32x32b.x16.b32 "
+                                     "{%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, [%16];"
+                                     : "=r"(v[0]), "=r"(v[1]), "=r"(v[2]), "=r"(v[3]), "=r"(v[4]), "=r"(v[5]),
+                                       "=r"(v[6]), "=r"(v[7]), "=r"(v[8]), "=r"(v[9]), "=r"(v[10]), "=r"(v[11]),
+                                       "=r"(v[12]), "=r"(v[13]), "=r"(v[14]), "=r"(v[15])
+                                     : "r"(taddr));
+                    } else {
+                        asm volatile("tcgen05.ld.sync.aligned.32x32b.x8.b32 {%0,%1,%2,%3,%4,%5,%6,%7}, [%8];"
+                                     : "=r"(v[0]), "=r"(v[1]), "=r"(v[2]), "=r"(v[3]), "=r"(v[4]), "=r"(v[5]),
+                                       "=r"(v[6]), "=r"(v[7])
+                                     : "r"(taddr));
+                    }
                     asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
                     // threshold on the scaled accumulator: D/2^8 < -x - H mu_i
                     const bool asset = row < n;
@@ -392,16 +415,16 @@ __global__ void __launch_bounds__(kTcThreads, 1) mc_tc_kernel(const __grid_const
                                             : 0.f;
                     int cnt = 0;
 #pragma unroll
-                    for (int c = 0; c < 16; c++) {
+                    for (int c = 0; c < kCols; c++) {
                         const float d = __uint_as_float(v[c]);
                         const unsigned m = __ballot_sync(0xffffffffu, asset && d < thr);
                         if (lane == c) cnt = __popc(m);
                     }
-                    if (lane < 16 && cnt) atomicAdd(&sS[sub * 16 + lane], cnt);
+                    if (lane < kCols && cnt) atomicAdd(&sS[sub * kCols + lane], cnt);
                     if (row == n) {
 #pragma unroll
-                        for (int c = 0; c < 16; c++)
-                            sPort[sub * 16 + c] = (float)(it.hwmu + (double)(__uint_as_float(v[c]) * (1.0f / kTcLScale)));
+                        for (int c = 0; c < kCols; c++)
+                            sPort[sub * kCols + c] = (float)(it.hwmu + (double)(__uint_as_float(v[c]) * (1.0f / kTcLScale)));
                     }
                 }
             }
@@ -560,7 +583,7 @@ cudaError_t launch_tc(const PlainArgs &a, const unsigned char *tiles, int bf16, 
     b.var = a;
     if (b.one.n_mt * kTcPaths > 512) return cudaErrorInvalidValue;
     const size_t smem = tc_smem_bytes(b.n_kt_max);
-    auto kern = (a.var_mode != 0) ? mc_tc_kernel<true> : mc_tc_kernel<false>;
+    auto kern = (a.var_mode != 0) ? mc_tc_kernel<true, false> : mc_tc_kernel<false, false>;
     cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess) return e;
     long long grid = sm_count;
@@ -600,7 +623,7 @@ cudaError_t launch_tc_batch(const void *d_items, int n_items, long long total_ti
     b.tmem_cols = tmem_cols_for(n_mt_max);
     if (n_mt_max * kTcPaths > 512 || n_kt_max > kTcMaxKt) return cudaErrorInvalidValue;
     const size_t smem = tc_smem_bytes(n_kt_max);
-    mc_tc_kernel<false><<<(unsigned)grid, kTcThreads, smem, s>>>(b);
+    mc_tc_kernel<false, true><<<(unsigned)grid, kTcThreads, smem, s>>>(b);
     return cudaGetLastError();
 }
 
@@ -609,7 +632,7 @@ cudaError_t launch_tc_batch(const void *d_items, int n_items, long long total_ti
 int tc_batch_occupancy(int n_kt_max)
 {
     int per_sm = 0;
-    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, mc_tc_kernel<false>, kTcThreads,
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, mc_tc_kernel<false, true>, kTcThreads,
                                                       tc_smem_bytes(n_kt_max)) != cudaSuccess)
         return 1;
     return per_sm < 1 ? 1 : per_sm;
@@ -619,7 +642,7 @@ int tc_batch_occupancy(int n_kt_max)
 // batch can ask for; called once before any launch or capture.
 cudaError_t tc_batch_prepare()
 {
-    return cudaFuncSetAttribute(mc_tc_kernel<false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+    return cudaFuncSetAttribute(mc_tc_kernel<false, true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                 (int)tc_smem_bytes(kTcMaxKt));
 }
 
