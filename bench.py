@@ -268,8 +268,9 @@ def engine_arm(args):
     prec = {"auto": riskgpu.PREC_AUTO, "fp32": riskgpu.PREC_FP32, "bf16x3": riskgpu.PREC_BF16X3,
             "fp16x3": riskgpu.PREC_FP16X3}[args.precision]
     draws = riskgpu.DRAWS_AGGREGATED if args.draw_mode == "aggregated" else riskgpu.DRAWS_DAILY
-    q = riskgpu.make_query(args.paths, p.seed, x=p.x, k=p.k, horizon=p.horizon,
-                           port_threshold=p.port_threshold, path_offset=rank * args.paths,
+    offset, count = riskgpu.shard_range(rank, world, args.paths)
+    q = riskgpu.make_query(count, p.seed, x=p.x, k=p.k, horizon=p.horizon,
+                           port_threshold=p.port_threshold, path_offset=offset,
                            precision=prec, draw_mode=draws)
 
     with torch.cuda.stream(stream):

@@ -399,6 +399,15 @@ def probe_peaks(stream=None) -> dict:
     return {f: getattr(pk, f) for f, _ in pk._fields_}
 
 
+def shard_range(rank: int, world: int, paths_per_rank: int):
+    """Path range of one rank in a weak-scaling run: rank r owns the paths
+    [r * paths_per_rank, (r + 1) * paths_per_rank) (counter-based draws: no
+    state moves between ranks; the only exchange is the sum of the counts)."""
+    if world < 1 or not (0 <= rank < world) or paths_per_rank < 1:
+        raise ValueError("bad shard")
+    return rank * paths_per_rank, paths_per_rank
+
+
 def estimator_stats(count, M):
     out = [ctypes.c_double() for _ in range(4)]
     lib().rg_estimator_stats(int(count), int(M), *[ctypes.byref(o) for o in out])
