@@ -46,9 +46,10 @@ sys.path.insert(0, os.path.join(ROOT, "gpu-montecarlo-risk_gb300"))
 METRIC = "paths_per_second"
 UNIT = "paths/s"
 
-# DRAM bytes per launch of the fused kernel measured by ncu on the full
-# workload (profiles/mc_plain_one_factor_50.md); None until captured.
-NCU_TRAFFIC_BYTES = None
+# DRAM bytes (read + write) per launch of the fused N=50 kernel from one ncu
+# capture (profiles/mc_rows_one_factor_50.md: 41.2 KB + 1.3 KB; it does not
+# grow with the paths per launch, only the factor and the counters move).
+NCU_TRAFFIC_BYTES = 42_496
 
 
 def parse():
@@ -342,16 +343,33 @@ def engine_arm(args):
     achieved = flops_per_path * args.paths / (ms_per_step * 1e-3) / 1e12
     t_ideal = (flops_per_path / (peaks["fp32_tflops"] * 1e12)
                + normals_per_path / peaks["normals_per_s"]) * args.paths
-    kname = ("rg::mc_rows_kernel<13,true,false> (N=50)" if n <= 64 else "rg::mc_tiled_kernel<false>")
-    roofline = {"bound": "alu", "kernel": kname,
-                "achieved": achieved, "peak": peaks["fp32_tflops"], "unit": "TFLOP/s",
-                "frac": achieved / peaks["fp32_tflops"],
-                "peak_source": "measured live: FP32 FMA micro-kernel (rg_probe_peaks)",
-                "composite_frac": t_ideal / (ms_per_step * 1e-3),
-                "normals_per_s": normals_per_path * args.paths / (ms_per_step * 1e-3),
-                "normals_peak": peaks["normals_per_s"],
-                "algorithmic_flops_per_path": flops_per_path,
-                "traffic": NCU_TRAFFIC_BYTES}
+    normals_per_s = normals_per_path * args.paths / (ms_per_step * 1e-3)
+    if prec in (riskgpu.PREC_FP16X3, riskgpu.PREC_BF16X3):
+        # tcgen05 form: the contraction runs on the tensor pipe (three split
+        # products); what bounds it is the normal generation on the ALU/XU
+        # pipes, so the roofline is normals/s against the measured generator
+        # peak, with the tensor-pipe rate beside it
+        kname = ("rg::mc_tc_kernel<false,false>" if args.draw_mode == "aggregated"
+                 else "rg::mc_tcws_kernel<false,false>")
+        roofline = {"bound": "alu", "kernel": kname,
+                    "achieved": normals_per_s, "peak": peaks["normals_per_s"], "unit": "normals/s",
+                    "frac": normals_per_s / peaks["normals_per_s"],
+                    "peak_source": "measured live: Philox4x32-10 + Box-Muller micro-kernel (rg_probe_peaks)",
+                    "tensor_tflops_useful_x3": 3 * achieved,
+                    "algorithmic_flops_per_path": flops_per_path,
+                    "normals_per_path": normals_per_path,
+                    "traffic": None}
+    else:
+        kname = ("rg::mc_rows_kernel<13,true,false> (N=50)" if n <= 64 else "rg::mc_tiled_kernel<false>")
+        roofline = {"bound": "alu", "kernel": kname,
+                    "achieved": achieved, "peak": peaks["fp32_tflops"], "unit": "TFLOP/s",
+                    "frac": achieved / peaks["fp32_tflops"],
+                    "peak_source": "measured live: FP32 FMA micro-kernel (rg_probe_peaks)",
+                    "composite_frac": t_ideal / (ms_per_step * 1e-3),
+                    "normals_per_s": normals_per_s,
+                    "normals_peak": peaks["normals_per_s"],
+                    "algorithmic_flops_per_path": flops_per_path,
+                    "traffic": NCU_TRAFFIC_BYTES if n <= 64 else None}
 
     line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": ms_per_step, "higher_is_better": True,

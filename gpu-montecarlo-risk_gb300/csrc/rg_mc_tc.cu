@@ -35,6 +35,7 @@
 // own copies and MMAs (again bounded), frees its tensor memory and returns;
 // the host reports RG_ERR_TIMEOUT.
 #include <cstdint>
+#include <cstdlib>
 #include <cstring>
 #include <cuda_fp16.h>
 #include <cuda_bf16.h>
@@ -99,6 +100,10 @@ __device__ __forceinline__ void mbar_expect_tx(uint64_t *bar, unsigned bytes)
 {
     asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar)), "r"(bytes)
                  : "memory");
+}
+__device__ __forceinline__ void mbar_arrive(uint64_t *bar)
+{
+    asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_u32(bar)) : "memory");
 }
 __device__ __forceinline__ bool mbar_try_wait(uint64_t *bar, unsigned parity)
 {
@@ -379,6 +384,9 @@ __global__ void __launch_bounds__(kTcThreads, 1) mc_tc_kernel(const __grid_const
                 tc_commit(&done_bar); // all MMAs of the tile issued so far
                 s_cons = cons_iter;
             }
+            // lanes 1-31 of warps 0 and 1 wait here, blocked, for their lane 0:
+            // spinning on done_bar beside it would take its issue slots
+            __syncwarp();
             // ---- 3. epilogue
             const bool done_ok = mbar_wait(&done_bar, tile_iter & 1u);
             if (!done_ok && tid == 0) {
@@ -465,6 +473,394 @@ __global__ void __launch_bounds__(kTcThreads, 1) mc_tc_kernel(const __grid_const
             // copies issued but not consumed: wait for them to land
             for (unsigned i = s_cons; i < prod_iter; i++)
                 mbar_wait(&full_bar[i % kTcStages], (i / kTcStages) & 1u);
+        }
+    }
+    tc_fence_before();
+    __syncthreads();
+    tc_fence_after();
+    if (warp == 0) asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(ncols));
+    if (VAR) cta_flush(a, 0, 0, n_tail, tail_fx, sacc, nullptr, true);
+}
+
+// ----------------------------------------------------------------------
+// Warp-specialised form of the same computation.  1024 threads:
+//   warps 0-3   (128 threads)  tensor-memory side: warp 0 lane 0 issues the
+//               MMAs, warp 1 lane 0 streams the Lhat tiles, all four warps
+//               run the epilogue (warp w reads TMEM lanes 32 w .. +31);
+//   warps 4-31  (896 threads)  generator: draw the normals of the NEXT tile
+//               one 64-column K tile at a time into the single Z buffer.
+// The MMAs run K-tile-outer (for each K tile, every row tile that needs
+// it), so K tile kt is released (zempty[kt], tcgen05.commit) as soon as its
+// MMAs are done and the generator may overwrite it for the next tile while
+// the remaining MMAs and the epilogue of the current tile proceed.
+// Barriers (all waits bounded):
+//   zfull[kt]  generator -> MMA: K tile kt of the next tile is written
+//              (its arrival for kt = 0 also publishes the tile index and item)
+//   zempty[kt] MMA -> generator: the MMAs that read K tile kt are complete
+//   full/empty L-tile ring as before; tfull: all MMAs of the tile complete
+//   slot_free[s] epilogue -> generator: the tile in slot s is finished, its
+//              item slot may be reused
+// Per-K-tile use counts (the same on both sides) give the mbarrier parities,
+// since items of a batch have different numbers of K tiles.
+static constexpr int kWsThreads = 1024;
+static constexpr int kWsTmemThreads = 128;
+static constexpr int kWsGenThreads = kWsThreads - kWsTmemThreads;
+
+__device__ __forceinline__ void named_sync(int id, int n)
+{
+    asm volatile("bar.sync %0, %1;" ::"r"(id), "r"(n) : "memory");
+}
+
+// named barrier that also ORs a predicate over the participating threads
+__device__ __forceinline__ int named_sync_or(int id, int n, int pred)
+{
+    int r;
+    asm volatile("{\n\t.reg .pred p, q;\n\tsetp.ne.s32 p, %1, 0;\n\tbar.red.or.pred q, %2, %3, p;\n\t"
+                 "selp.s32 %0, 1, 0, q;\n\t}"
+                 : "=r"(r)
+                 : "r"(pred), "r"(id), "r"(n)
+                 : "memory");
+    return r;
+}
+
+template <bool VAR, bool BATCH>
+__global__ void __launch_bounds__(kWsThreads, 1) mc_tcws_kernel(const __grid_constant__ TcBatch b)
+{
+    extern __shared__ __align__(1024) unsigned char tc_smem[];
+    const PlainArgs &a = b.var;
+    unsigned char *base = (unsigned char *)(((uintptr_t)tc_smem + 1023) & ~(uintptr_t)1023);
+    unsigned char *zhi = base;
+    unsigned char *zlo = zhi + b.n_kt_max * kTcZBytes;
+    unsigned char *lst = zlo + b.n_kt_max * kTcZBytes;
+
+    __shared__ __align__(8) uint64_t full_bar[kTcStages], empty_bar[kTcStages], tfull_bar;
+    __shared__ __align__(8) uint64_t zfull[kTcMaxKt], zempty[kTcMaxKt], slot_free[2];
+    __shared__ uint32_t tmem_base_sh;
+    __shared__ int sS[kTcPaths];
+    __shared__ float sPort[kTcPaths];
+    // abort flag of the tensor-memory side: written by its threads before a
+    // group barrier and read after it, so every decision taken on it is
+    // uniform across the group (the generator only skips waits on it)
+    __shared__ int tm_abort;
+    __shared__ long long s_tile[2];
+    __shared__ long long s_unit;
+    __shared__ unsigned long long sacc[4];
+    __shared__ __align__(16) TcItem s_item[BATCH ? 2 : 1];
+
+    const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+    const int ncols = b.tmem_cols;
+    if (tid < 4) sacc[tid] = 0ull;
+    if (tid < kTcPaths) {
+        sS[tid] = 0;
+        sPort[tid] = 0.f;
+    }
+    if (tid == 0) {
+        for (int s = 0; s < kTcStages; s++) {
+            mbar_init(&full_bar[s], 1);
+            mbar_init(&empty_bar[s], 1);
+        }
+        for (int k = 0; k < kTcMaxKt; k++) {
+            mbar_init(&zfull[k], kWsGenThreads); // every generator thread arrives once per tile
+            mbar_init(&zempty[k], 1);
+        }
+        mbar_init(&slot_free[0], 1);
+        mbar_init(&slot_free[1], 1);
+        mbar_init(&tfull_bar, 1);
+        tm_abort = 0;
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    }
+    if (warp == 0) {
+        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(&tmem_base_sh)),
+                     "r"(ncols));
+        asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;");
+    }
+    tc_fence_before();
+    __syncthreads();
+    tc_fence_after();
+    const uint32_t tmem = tmem_base_sh;
+    const long long total = b.dyn ? b.dyn[1] : b.total_tiles;
+    const int n_items = b.dyn ? (int)b.dyn[0] : b.n_items;
+    // bit kt = parity of the number of tiles so far that used K tile kt (the
+    // same on both sides; it selects the mbarrier phase to wait for)
+    unsigned zpar = 0;
+    int n_tail = 0;
+    long long tail_fx = 0;
+
+    if (warp >= kWsTmemThreads / 32) {
+        // ======================= generator =======================
+        // gab: this thread's abort flag. Threads of the group do not meet at
+        // K-tile boundaries, so a timeout is first local; the reduction barrier
+        // at the start of each tile makes it uniform before any decision that
+        // changes barrier participation.
+        const int gtid = tid - kWsTmemThreads;
+        int gab = 0;
+        long long unit = -1, unit_end = 0, next_static = blockIdx.x;
+        for (unsigned j = 0;; j++) {
+            const int slot = j & 1;
+            // the item slot must be free (epilogue of tile j-2 done); after an
+            // abort on either side no wait is made (only barrier order is kept)
+            if (!gab && !tm_abort && !mbar_wait(&slot_free[slot], ((j >> 1) & 1u) ^ 1u)) {
+                atomicOr(b.err, 8u);
+                gab = 1;
+            }
+            gab = named_sync_or(2, kWsGenThreads, gab);
+            if (gtid == 0) {
+                long long tile = -1;
+                if (!gab && !tm_abort) {
+                    if (b.work) {
+                        if (unit < 0 || unit_end <= 0) {
+                            unit = (long long)atomicAdd(b.work, 1u);
+                            unit_end = b.unit_tiles;
+                        }
+                        tile = unit * b.unit_tiles + (b.unit_tiles - unit_end);
+                        unit_end--;
+                        if (tile >= total || unit * b.unit_tiles >= total) tile = -1;
+                    } else {
+                        tile = next_static;
+                        next_static += gridDim.x;
+                        if (tile >= total) tile = -1;
+                    }
+                }
+                s_tile[slot] = tile;
+                if (BATCH && tile >= 0) {
+                    int lo = 0, hi = n_items - 1;
+                    while (lo < hi) {
+                        const int mid = (lo + hi + 1) >> 1;
+                        if (b.items[mid].tile_begin <= tile) lo = mid; else hi = mid - 1;
+                    }
+                    s_unit = lo;
+                }
+            }
+            named_sync(2, kWsGenThreads);
+            const long long tile = s_tile[slot];
+            if (BATCH && tile >= 0) { // stage the item in its slot
+                const int *src = reinterpret_cast<const int *>(&b.items[s_unit]);
+                int *dst = reinterpret_cast<int *>(&s_item[slot]);
+                for (int w = gtid; w < (int)(sizeof(TcItem) / 4); w += kWsGenThreads) dst[w] = src[w];
+                named_sync(2, kWsGenThreads);
+            }
+            if (tile < 0) { // uniform: gtid 0 publishes -1 after any abort
+                // publish the end (after the MMA side consumed K tile 0 of the last tile)
+                if (!gab && !tm_abort && !mbar_wait(&zempty[0], (zpar & 1u) ^ 1u)) gab = 1;
+                mbar_arrive(&zfull[0]); // every generator thread: completes the phase
+                break;
+            }
+            const TcItem &it = BATCH ? s_item[slot] : b.one;
+            const int n = it.n, nq = (n + 3) >> 2, n_kt = it.n_kt;
+            const long long p0 = (tile - it.tile_begin) * kTcPaths;
+            // each thread walks its items of the tile in K-tile order and
+            // arrives on zfull[kt] once it has written its share of kt (no
+            // group barrier, so no thread idles at K-tile boundaries)
+            for (int kt = 0; kt < n_kt; kt++) {
+                // the previous tile's MMAs on this K tile are done
+                if (!gab && !tm_abort && !mbar_wait(&zempty[kt], ((zpar >> kt) & 1u) ^ 1u)) {
+                    atomicOr(b.err, 16u);
+                    gab = 1;
+                }
+                const int per_kt = kTcPaths * (kTcKt / 4);
+                // items of this thread in kt: global item index i = kt*per_kt + local,
+                // assigned round robin over the whole tile (i % kWsGenThreads == gtid)
+                int first = gtid - (kt * per_kt) % kWsGenThreads;
+                if (first < 0) first += kWsGenThreads;
+                for (int item = first; item < per_kt; item += kWsGenThreads) {
+                    const int p = item & (kTcPaths - 1), q = kt * (kTcKt / 4) + (item >> 6);
+                    const unsigned long long path = it.path0 + (unsigned long long)(p0 + p);
+                    const uint32_t plo = (uint32_t)path, phi = (uint32_t)(path >> 32);
+                    float z[4] = {0.f, 0.f, 0.f, 0.f};
+                    if (q < nq) {
+                        const int days = it.aggregated ? 1 : it.horizon;
+                        for (int d = 0; d < days; d++) {
+                            const uint4 wv = rg_philox(make_uint4((uint32_t)(d * nq + q), 0u, plo, phi), it.keys);
+                            float z0, z1, z2, z3;
+                            rg_box_muller(wv.x, wv.y, z0, z1);
+                            rg_box_muller(wv.z, wv.w, z2, z3);
+                            z[0] += z0;
+                            z[1] += z1;
+                            z[2] += z2;
+                            z[3] += z3;
+                        }
+                        if (it.aggregated)
+                            for (int e = 0; e < 4; e++) z[e] *= it.sqrt_h;
+                    }
+                    unsigned short h[4], l[4];
+                    for (int e = 0; e < 4; e++) split2(z[e], it.bf16, h[e], l[e]);
+                    const uint32_t off = (uint32_t)kt * kTcZBytes + sw128_offset(p, 4 * (item >> 6));
+                    *reinterpret_cast<uint2 *>(zhi + off) =
+                        make_uint2((uint32_t)h[0] | ((uint32_t)h[1] << 16), (uint32_t)h[2] | ((uint32_t)h[3] << 16));
+                    *reinterpret_cast<uint2 *>(zlo + off) =
+                        make_uint2((uint32_t)l[0] | ((uint32_t)l[1] << 16), (uint32_t)l[2] | ((uint32_t)l[3] << 16));
+                }
+                fence_async_shared(); // this thread's writes -> async proxy (tensor cores)
+                mbar_arrive(&zfull[kt]);
+                zpar ^= 1u << kt;
+            }
+        }
+    } else {
+        // ======================= tensor-memory side =======================
+        unsigned prod_iter = 0, cons_iter = 0;
+        for (unsigned j = 0;; j++) {
+            const int slot = j & 1;
+            // K tile 0 of tile j is written and its index published
+            if (!mbar_wait(&zfull[0], zpar & 1u)) {
+                atomicOr(b.err, 32u);
+                tm_abort = 1;
+            }
+            named_sync(1, kWsTmemThreads);
+            const long long tile = s_tile[slot];
+            if (tile < 0 || tm_abort) break; // uniform: both read after the group barrier
+            const TcItem &it = BATCH ? s_item[slot] : b.one;
+            const int n = it.n, n_kt = it.n_kt, n_mt = it.n_mt;
+            tc_fence_after();
+            if (warp == 1 && lane == 0) {
+                // producer: Lhat tiles in (K tile, row tile) order
+                for (int kt = 0; kt < n_kt && !tm_abort; kt++) {
+                    for (int mt = 0; mt < n_mt; mt++) {
+                        const int kts = (mt == n_mt - 1) ? n_kt : min(n_kt, (kTcRows * (mt + 1) + kTcKt - 1) / kTcKt);
+                        if (kt >= kts) continue;
+                        const int s = prod_iter % kTcStages;
+                        if (!mbar_wait(&empty_bar[s], ((prod_iter / kTcStages) & 1u) ^ 1u)) {
+                            atomicOr(b.err, 1u);
+                            tm_abort = 1;
+                            break;
+                        }
+                        if (b.inject_stall && prod_iter == 1) { // never filled: the consumer's wait runs out
+                            prod_iter++;
+                            continue;
+                        }
+                        mbar_expect_tx(&full_bar[s], 2 * kTcTileBytes);
+                        const unsigned char *src = it.tiles + ((size_t)(mt * n_kt + kt) * 2) * kTcTileBytes;
+                        unsigned char *dst = lst + (size_t)s * 2 * kTcTileBytes;
+                        bulk_copy(dst, src, kTcTileBytes, &full_bar[s]);
+                        bulk_copy(dst + kTcTileBytes, src + kTcTileBytes, kTcTileBytes, &full_bar[s]);
+                        prod_iter++;
+                    }
+                }
+            } else if (warp == 0 && lane == 0) {
+                // MMA issuer, K-tile-outer
+                const uint32_t idesc = tc_idesc(it.bf16, kTcRows, kTcPaths);
+                for (int kt = 0; kt < n_kt && !tm_abort; kt++) {
+                    if (kt > 0 && !mbar_wait(&zfull[kt], (zpar >> kt) & 1u)) {
+                        atomicOr(b.err, 64u);
+                        tm_abort = 1;
+                        break;
+                    }
+                    tc_fence_after();
+                    const uint32_t zh = smem_u32(zhi + (size_t)kt * kTcZBytes);
+                    const uint32_t zl = smem_u32(zlo + (size_t)kt * kTcZBytes);
+                    for (int mt = 0; mt < n_mt; mt++) {
+                        const int kts = (mt == n_mt - 1) ? n_kt : min(n_kt, (kTcRows * (mt + 1) + kTcKt - 1) / kTcKt);
+                        if (kt >= kts) continue;
+                        const int s = cons_iter % kTcStages;
+                        if (!mbar_wait(&full_bar[s], (cons_iter / kTcStages) & 1u)) {
+                            atomicOr(b.err, 2u);
+                            tm_abort = 1;
+                            break;
+                        }
+                        tc_fence_after();
+                        const uint32_t lhi = smem_u32(lst + (size_t)s * 2 * kTcTileBytes);
+                        const uint32_t llo = lhi + kTcTileBytes;
+                        const uint32_t d_tmem = tmem + (uint32_t)(mt * kTcPaths);
+#pragma unroll
+                        for (int ks = 0; ks < kTcKt / 16; ks++) {
+                            const uint32_t o = (uint32_t)ks * 32;
+                            const uint32_t acc0 = (kt > 0 || ks > 0) ? 1u : 0u;
+                            tc_mma(d_tmem, sw128_desc(lhi + o), sw128_desc(zh + o), idesc, acc0);
+                            tc_mma(d_tmem, sw128_desc(lhi + o), sw128_desc(zl + o), idesc, 1u);
+                            tc_mma(d_tmem, sw128_desc(llo + o), sw128_desc(zh + o), idesc, 1u);
+                        }
+                        tc_commit(&empty_bar[s]);
+                        cons_iter++;
+                    }
+                    tc_commit(&zempty[kt]); // K tile kt may be overwritten once these MMAs complete
+                }
+                tc_commit(&tfull_bar);
+            }
+            // lanes 1-31 of warps 0 and 1 wait here, blocked, for their lane 0
+            // (the producer and the MMA issuer): spinning on tfull_bar beside
+            // it would take its issue slots
+            __syncwarp();
+            // per-K-tile use parities advance on this side too
+            zpar ^= (1u << n_kt) - 1u;
+            // ---- epilogue (warps 0-3)
+            if (!mbar_wait(&tfull_bar, j & 1u)) {
+                atomicOr(b.err, 4u);
+                tm_abort = 1;
+            }
+            tc_fence_after();
+            named_sync(1, kWsTmemThreads);
+            if (!tm_abort) {
+                const int quarter = warp; // lanes 32*warp .. +31
+                for (int mt = 0; mt < n_mt; mt++) {
+                    const int row = mt * kTcRows + quarter * 32 + lane;
+                    const bool asset = row < n;
+                    const float thr = asset ? (float)(((double)it.neg_x - (double)it.horizon * it.mu64[row]) * kTcLScale)
+                                            : 0.f;
+#pragma unroll
+                    for (int cb = 0; cb < kTcPaths / 16; cb++) {
+                        const uint32_t taddr = tmem + ((uint32_t)(quarter * 32) << 16) + (uint32_t)(mt * kTcPaths + cb * 16);
+                        uint32_t v[16];
+                        asm volatile("tcgen05.ld.sync.aligned.32x32b.x16.b32 "
+                                     "{%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, [%16];"
+                                     : "=r"(v[0]), "=r"(v[1]), "=r"(v[2]), "=r"(v[3]), "=r"(v[4]), "=r"(v[5]),
+                                       "=r"(v[6]), "=r"(v[7]), "=r"(v[8]), "=r"(v[9]), "=r"(v[10]), "=r"(v[11]),
+                                       "=r"(v[12]), "=r"(v[13]), "=r"(v[14]), "=r"(v[15])
+                                     : "r"(taddr));
+                        asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+                        int cnt = 0;
+#pragma unroll
+                        for (int c = 0; c < 16; c++) {
+                            const unsigned m = __ballot_sync(0xffffffffu, asset && __uint_as_float(v[c]) < thr);
+                            if (lane == c) cnt = __popc(m);
+                        }
+                        if (lane < 16 && cnt) atomicAdd(&sS[cb * 16 + lane], cnt);
+                        if (row == n) {
+#pragma unroll
+                            for (int c = 0; c < 16; c++)
+                                sPort[cb * 16 + c] =
+                                    (float)(it.hwmu + (double)(__uint_as_float(v[c]) * (1.0f / kTcLScale)));
+                        }
+                    }
+                }
+            }
+            tc_fence_before();
+            named_sync(1, kWsTmemThreads);
+            if (!tm_abort && tid < kTcPaths) {
+                const long long p = (tile - it.tile_begin) * kTcPaths + tid;
+                int crash = 0, breach = 0;
+                if (p < it.n_paths) {
+                    const int S = sS[tid];
+                    const float port = sPort[tid];
+                    crash = (S >= it.k) ? 1 : 0;
+                    breach = (it.has_w && port < it.port_thr) ? 1 : 0;
+                    if (it.s_values) it.s_values[p] = S;
+                    if (it.port_values) it.port_values[p] = port;
+                    if (VAR) var_path(a, port, nullptr, n_tail, tail_fx);
+                }
+                crash = __reduce_add_sync(0xffffffffu, crash);
+                breach = __reduce_add_sync(0xffffffffu, breach);
+                if (lane == 0) {
+                    if (crash) atomicAdd(&it.counts[0], (unsigned long long)crash);
+                    if (breach) atomicAdd(&it.counts[1], (unsigned long long)breach);
+                }
+            }
+            if (tid < kTcPaths) {
+                sS[tid] = 0;
+                sPort[tid] = 0.f;
+            }
+            named_sync(1, kWsTmemThreads);
+            tc_fence_after();
+            if (tid == 0) mbar_arrive(&slot_free[slot]); // the generator may reuse this item slot
+        }
+        // drain on abort: MMAs and copies issued but not waited for
+        if (tm_abort) {
+            if (warp == 0 && lane == 0) {
+                tc_commit(&tfull_bar);
+                mbar_wait(&tfull_bar, 0u);
+                mbar_wait(&tfull_bar, 1u);
+            }
+            if (warp == 1 && lane == 0)
+                for (unsigned i = cons_iter; i < prod_iter; i++)
+                    mbar_wait(&full_bar[i % kTcStages], (i / kTcStages) & 1u);
         }
     }
     tc_fence_before();
@@ -583,12 +979,22 @@ cudaError_t launch_tc(const PlainArgs &a, const unsigned char *tiles, int bf16, 
     b.var = a;
     if (b.one.n_mt * kTcPaths > 512) return cudaErrorInvalidValue;
     const size_t smem = tc_smem_bytes(b.n_kt_max);
-    auto kern = (a.var_mode != 0) ? mc_tc_kernel<true, false> : mc_tc_kernel<false, false>;
+    // Daily draws: the warp-specialised kernel (generation, which dominates,
+    // overlaps the MMAs and the epilogue).  Aggregated draws: generation is
+    // cheap and the single TMEM accumulator serialises MMAs and epilogue, so
+    // the phase-serial kernel, whose epilogue runs on all 16 warps, is faster.
+    // RG_TC_KERNEL=simple|ws overrides the choice.
+    const char *sel = getenv("RG_TC_KERNEL");
+    bool simple = aggregated;
+    if (sel && strstr(sel, "simple")) simple = true;
+    if (sel && strstr(sel, "ws")) simple = false;
+    auto kern = simple ? ((a.var_mode != 0) ? mc_tc_kernel<true, false> : mc_tc_kernel<false, false>)
+                       : ((a.var_mode != 0) ? mc_tcws_kernel<true, false> : mc_tcws_kernel<false, false>);
     cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess) return e;
     long long grid = sm_count;
     if (b.total_tiles < grid) grid = b.total_tiles;
-    kern<<<(unsigned)grid, kTcThreads, smem, s>>>(b);
+    kern<<<(unsigned)grid, simple ? kTcThreads : kWsThreads, smem, s>>>(b);
     return cudaGetLastError();
 }
 
@@ -623,7 +1029,7 @@ cudaError_t launch_tc_batch(const void *d_items, int n_items, long long total_ti
     b.tmem_cols = tmem_cols_for(n_mt_max);
     if (n_mt_max * kTcPaths > 512 || n_kt_max > kTcMaxKt) return cudaErrorInvalidValue;
     const size_t smem = tc_smem_bytes(n_kt_max);
-    mc_tc_kernel<false, true><<<(unsigned)grid, kTcThreads, smem, s>>>(b);
+    mc_tcws_kernel<false, true><<<(unsigned)grid, kWsThreads, smem, s>>>(b);
     return cudaGetLastError();
 }
 
@@ -632,7 +1038,7 @@ cudaError_t launch_tc_batch(const void *d_items, int n_items, long long total_ti
 int tc_batch_occupancy(int n_kt_max)
 {
     int per_sm = 0;
-    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, mc_tc_kernel<false, true>, kTcThreads,
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, mc_tcws_kernel<false, true>, kWsThreads,
                                                       tc_smem_bytes(n_kt_max)) != cudaSuccess)
         return 1;
     return per_sm < 1 ? 1 : per_sm;
@@ -642,7 +1048,7 @@ int tc_batch_occupancy(int n_kt_max)
 // batch can ask for; called once before any launch or capture.
 cudaError_t tc_batch_prepare()
 {
-    return cudaFuncSetAttribute(mc_tc_kernel<false, true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+    return cudaFuncSetAttribute(mc_tcws_kernel<false, true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                 (int)tc_smem_bytes(kTcMaxKt));
 }
 

@@ -36,9 +36,17 @@ def _case(n, seed):
     return mu, sigma, w
 
 
+# the two tcgen05 kernels: "ws" (warp-specialised, chosen for daily draws)
+# and "simple" (phase-serial, chosen for aggregated draws); RG_TC_KERNEL
+# forces one of them
+KERNELS = ["ws", "simple"]
+
+
+@pytest.mark.parametrize("kernel", KERNELS)
 @pytest.mark.parametrize("prec", ["fp16x3", "bf16x3"])
 @pytest.mark.parametrize("n,horizon,M", [(16, 1, 256), (64, 1, 1000), (130, 2, 777), (600, 10, 256)])
-def test_tc_per_path_parity(gpu, oracle, prec, n, horizon, M):
+def test_tc_per_path_parity(gpu, oracle, monkeypatch, kernel, prec, n, horizon, M):
+    monkeypatch.setenv("RG_TC_KERNEL", kernel)
     code, near_tol, port_tol = CASES[prec]
     mu, sigma, w = _case(n, n + 1)
     x, k, thr, seed = 0.02 * math.sqrt(horizon), max(1, n // 10), -0.03, 5 + n
@@ -55,7 +63,8 @@ def test_tc_per_path_parity(gpu, oracle, prec, n, horizon, M):
     assert r["breach_count"] == int((W < thr).sum())
 
 
-def test_tc_bounded_wait_reports_timeout(gpu, monkeypatch):
+@pytest.mark.parametrize("kernel", KERNELS)
+def test_tc_bounded_wait_reports_timeout(gpu, monkeypatch, kernel):
     """Failure detection without a GPU fault: with RG_FAULT_INJECT=tcstall
     one pipeline stage is never filled, the kernel's bounded wait (2 s) runs
     out, it drains its own copies and MMAs, frees its tensor memory and sets
@@ -64,6 +73,7 @@ def test_tc_bounded_wait_reports_timeout(gpu, monkeypatch):
     mu, sigma, w = _case(200, 3)
     port = gpu.Portfolio(mu, sigma, w)
     q = gpu.make_query(4096, 1, x=0.02, k=5, precision=3)
+    monkeypatch.setenv("RG_TC_KERNEL", kernel)
     monkeypatch.setenv("RG_FAULT_INJECT", "tcstall")
     with pytest.raises(gpu.RiskGpuError) as e:
         port.simulate(q)
@@ -73,10 +83,12 @@ def test_tc_bounded_wait_reports_timeout(gpu, monkeypatch):
     assert r["n_paths"] == 4096
 
 
+@pytest.mark.parametrize("kernel", KERNELS)
 @pytest.mark.parametrize("prec", ["fp16x3", "bf16x3"])
-def test_tc_var_and_aggregated(gpu, oracle, prec):
+def test_tc_var_and_aggregated(gpu, oracle, monkeypatch, kernel, prec):
     """VaR/CVaR order statistics of the tensor-core form equal those of its
     own per-path returns; aggregated draws match the oracle per path."""
+    monkeypatch.setenv("RG_TC_KERNEL", kernel)
     code, near_tol, port_tol = CASES[prec]
     mu, sigma, w = _case(300, 11)
     port = gpu.Portfolio(mu, sigma, w)
