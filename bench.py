@@ -349,8 +349,7 @@ def engine_arm(args):
         # products); what bounds it is the normal generation on the ALU/XU
         # pipes, so the roofline is normals/s against the measured generator
         # peak, with the tensor-pipe rate beside it
-        kname = ("rg::mc_tc_kernel<false,false>" if args.draw_mode == "aggregated"
-                 else "rg::mc_tcws_kernel<false,false>")
+        kname = "rg::mc_tcws_kernel<false,false>"
         roofline = {"bound": "alu", "kernel": kname,
                     "achieved": normals_per_s, "peak": peaks["normals_per_s"], "unit": "normals/s",
                     "frac": normals_per_s / peaks["normals_per_s"],

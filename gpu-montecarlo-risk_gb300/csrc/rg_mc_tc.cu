@@ -70,7 +70,7 @@ struct TcItem {
     PhiloxKeys keys;
     double hwmu;                  // H w.mu
     int n, n_mt, n_kt, horizon, k, has_w, aggregated, bf16;
-    float neg_x, port_thr, sqrt_h, pad_;
+    float neg_x, port_thr, sqrt_h, hwmu_f;  // hwmu_f = (float) hwmu
 };
 
 struct TcBatch {
@@ -88,6 +88,15 @@ struct TcBatch {
                               // (a graph captured once serves batches of any size)
     PlainArgs var;            // VaR fields of a single-item query (var_mode 0 otherwise)
 };
+
+// Scaled crash threshold of asset row r: the accumulator D = 2^8 (L Z)_r is
+// compared with 2^8 (-x - H mu_r).  FP32 throughout, like the epilogue's
+// portfolio value: this part's FP64 pipe is narrow, and one FP32 rounding
+// of these terms is far below the tensor-core form's own error.
+__device__ __forceinline__ float tc_threshold(const TcItem &it, int r)
+{
+    return (it.neg_x - (float)it.horizon * (float)it.mu64[r]) * kTcLScale;
+}
 
 // ------------------------------------------------------------ PTX wrappers
 __device__ __forceinline__ uint32_t smem_u32(const void *p) { return (uint32_t)__cvta_generic_to_shared(p); }
@@ -126,6 +135,7 @@ __device__ __forceinline__ unsigned long long global_ns()
 // kTcSpinLimit polls, whichever comes first.
 __device__ __forceinline__ bool mbar_wait(uint64_t *bar, unsigned parity)
 {
+    if (mbar_try_wait(bar, parity)) return true; // common case: no timer read
     const unsigned long long t0 = global_ns();
     for (unsigned i = 0; i < kTcSpinLimit; i++) {
         if (mbar_try_wait(bar, parity)) return true;
@@ -146,7 +156,7 @@ __device__ __forceinline__ void tc_fence_after() { asm volatile("tcgen05.fence::
 
 // Shared-memory matrix descriptor: K-major, 128-byte swizzle, 8-row groups
 // 1024 bytes apart.
-__device__ __forceinline__ uint64_t sw128_desc(uint32_t addr)
+__host__ __device__ constexpr uint64_t sw128_desc(uint32_t addr)
 {
     uint64_t d = 0;
     d |= (uint64_t)((addr & 0x3FFFFu) >> 4);  // start address
@@ -156,6 +166,14 @@ __device__ __forceinline__ uint64_t sw128_desc(uint32_t addr)
     d |= (uint64_t)2 << 61;                   // 128-byte swizzle
     return d;
 }
+
+// The same descriptor as two words: the high word is constant and the low
+// word is (address >> 4) | leading-byte-offset field, so an address step of
+// 16 n bytes is + n on the low word (shared addresses stay below 2^18).
+static constexpr uint32_t kSw128DescHi = (uint32_t)(sw128_desc(0u) >> 32);
+__host__ __device__ constexpr uint32_t sw128_desc_lo(uint32_t addr) { return (uint32_t)sw128_desc(addr); }
+static_assert(((uint64_t)kSw128DescHi << 32 | sw128_desc_lo(0x12340u)) == sw128_desc(0x12340u), "descriptor split");
+static_assert(sw128_desc_lo(0x12340u + 32u) == sw128_desc_lo(0x12340u) + 2u, "K step on the low word");
 
 // Instruction descriptor of kind::f16: FP32 accumulator, A and B of the same
 // type (FP16 or BF16), both K-major, M x N.
@@ -172,6 +190,40 @@ __device__ __forceinline__ void tc_mma(uint32_t d_tmem, uint64_t a_desc, uint64_
                  "setp.ne.b32 p, %4, 0;\n\t"
                  "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n\t}" ::"r"(d_tmem),
                  "l"(a_desc), "l"(b_desc), "r"(idesc), "r"(accumulate));
+}
+// The 12 MMAs of one (row tile, K tile) pair in one block: for each of the
+// four 16-element K steps, Lhi.Zhi (accumulating unless acc_first == 0 on the
+// first step), Lhi.Zlo and Llo.Zhi.  Descriptors are passed as their low
+// words (sw128_desc_lo); a K step is 32 bytes (+2), the lo part of an Lhat
+// tile 16 KB (+1024) further.
+__device__ __forceinline__ void tc_mma_pair(uint32_t d_tmem, uint32_t a_lo, uint32_t zh_lo, uint32_t zl_lo,
+                                            uint32_t idesc, uint32_t acc_first)
+{
+    asm volatile("{\n\t.reg .pred p, q;\n\t.reg .b32 ta, tl, th, tz;\n\t.reg .b64 da, dl, dh, dz;\n\t"
+                 "setp.ne.b32 p, %5, 0;\n\t"
+                 "setp.eq.b32 q, %5, %5;\n\t"
+                 "add.u32 ta, %1, 0;\n\tadd.u32 tl, %1, 1024;\n\tadd.u32 th, %2, 0;\n\tadd.u32 tz, %3, 0;\n\t"
+                 "mov.b64 da, {ta, %6};\n\tmov.b64 dl, {tl, %6};\n\tmov.b64 dh, {th, %6};\n\tmov.b64 dz, {tz, %6};\n\t"
+                 "tcgen05.mma.cta_group::1.kind::f16 [%0], da, dh, %4, p;\n\t"
+                 "tcgen05.mma.cta_group::1.kind::f16 [%0], da, dz, %4, q;\n\t"
+                 "tcgen05.mma.cta_group::1.kind::f16 [%0], dl, dh, %4, q;\n\t"
+                 "add.u32 ta, %1, 2;\n\tadd.u32 tl, %1, 1026;\n\tadd.u32 th, %2, 2;\n\tadd.u32 tz, %3, 2;\n\t"
+                 "mov.b64 da, {ta, %6};\n\tmov.b64 dl, {tl, %6};\n\tmov.b64 dh, {th, %6};\n\tmov.b64 dz, {tz, %6};\n\t"
+                 "tcgen05.mma.cta_group::1.kind::f16 [%0], da, dh, %4, q;\n\t"
+                 "tcgen05.mma.cta_group::1.kind::f16 [%0], da, dz, %4, q;\n\t"
+                 "tcgen05.mma.cta_group::1.kind::f16 [%0], dl, dh, %4, q;\n\t"
+                 "add.u32 ta, %1, 4;\n\tadd.u32 tl, %1, 1028;\n\tadd.u32 th, %2, 4;\n\tadd.u32 tz, %3, 4;\n\t"
+                 "mov.b64 da, {ta, %6};\n\tmov.b64 dl, {tl, %6};\n\tmov.b64 dh, {th, %6};\n\tmov.b64 dz, {tz, %6};\n\t"
+                 "tcgen05.mma.cta_group::1.kind::f16 [%0], da, dh, %4, q;\n\t"
+                 "tcgen05.mma.cta_group::1.kind::f16 [%0], da, dz, %4, q;\n\t"
+                 "tcgen05.mma.cta_group::1.kind::f16 [%0], dl, dh, %4, q;\n\t"
+                 "add.u32 ta, %1, 6;\n\tadd.u32 tl, %1, 1030;\n\tadd.u32 th, %2, 6;\n\tadd.u32 tz, %3, 6;\n\t"
+                 "mov.b64 da, {ta, %6};\n\tmov.b64 dl, {tl, %6};\n\tmov.b64 dh, {th, %6};\n\tmov.b64 dz, {tz, %6};\n\t"
+                 "tcgen05.mma.cta_group::1.kind::f16 [%0], da, dh, %4, q;\n\t"
+                 "tcgen05.mma.cta_group::1.kind::f16 [%0], da, dz, %4, q;\n\t"
+                 "tcgen05.mma.cta_group::1.kind::f16 [%0], dl, dh, %4, q;\n\t"
+                 "}"
+                 ::"r"(d_tmem), "r"(a_lo), "r"(zh_lo), "r"(zl_lo), "r"(idesc), "r"(acc_first), "r"(kSw128DescHi));
 }
 __device__ __forceinline__ void tc_commit(uint64_t *bar)
 {
@@ -419,8 +471,7 @@ __global__ void __launch_bounds__(kTcThreads, 1) mc_tc_kernel(const __grid_const
                     asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
                     // threshold on the scaled accumulator: D/2^8 < -x - H mu_i
                     const bool asset = row < n;
-                    const float thr = asset ? (float)(((double)it.neg_x - (double)it.horizon * it.mu64[row]) * kTcLScale)
-                                            : 0.f;
+                    const float thr = asset ? tc_threshold(it, row) : 0.f;
                     int cnt = 0;
 #pragma unroll
                     for (int c = 0; c < kCols; c++) {
@@ -432,7 +483,7 @@ __global__ void __launch_bounds__(kTcThreads, 1) mc_tc_kernel(const __grid_const
                     if (row == n) {
 #pragma unroll
                         for (int c = 0; c < kCols; c++)
-                            sPort[sub * kCols + c] = (float)(it.hwmu + (double)(__uint_as_float(v[c]) * (1.0f / kTcLScale)));
+                            sPort[sub * kCols + c] = it.hwmu_f + __uint_as_float(v[c]) * (1.0f / kTcLScale);
                     }
                 }
             }
@@ -483,28 +534,46 @@ __global__ void __launch_bounds__(kTcThreads, 1) mc_tc_kernel(const __grid_const
 }
 
 // ----------------------------------------------------------------------
-// Warp-specialised form of the same computation.  1024 threads:
-//   warps 0-3   (128 threads)  tensor-memory side: warp 0 lane 0 issues the
-//               MMAs, warp 1 lane 0 streams the Lhat tiles, all four warps
-//               run the epilogue (warp w reads TMEM lanes 32 w .. +31);
-//   warps 4-31  (896 threads)  generator: draw the normals of the NEXT tile
-//               one 64-column K tile at a time into the single Z buffer.
-// The MMAs run K-tile-outer (for each K tile, every row tile that needs
-// it), so K tile kt is released (zempty[kt], tcgen05.commit) as soon as its
-// MMAs are done and the generator may overwrite it for the next tile while
-// the remaining MMAs and the epilogue of the current tile proceed.
+// Warp-specialised form of the same computation.  1024 threads, four roles:
+//   warps 0-3    epilogue: warp w reads TMEM lanes 32 w .. +31 of a row tile
+//                as soon as that row tile is fully accumulated;
+//   warp 4       lane 0 issues the MMAs;
+//   warp 5       lane 0 streams the Lhat tiles into the ring;
+//   warps 6-31   (832 threads) generator: draws the normals one 64-column K
+//                tile at a time into a ring of kWsZSlots K-tile slots.
+// The MMAs run K-tile-outer (for each K tile, every row tile that needs it),
+// so a K tile is needed only while its MMAs run: K tiles are numbered in
+// order across the CTA's path tiles (g), K tile g lives in slot g % kWsZSlots
+// and the slot is released (zempty) as soon as its MMAs complete.  A ring of
+// four slots (64 KB) instead of a whole path tile's normals (160 KB) leaves
+// room for a five-stage Lhat ring, which hides the L2 latency of the copies.  Row tile
+// m is complete after K tile kts(m) - 1 (lower triangle), so its epilogue runs
+// while later K tiles are still being drawn, and the next tile's MMAs
+// overwrite its accumulator once the epilogue has read it (acc_free): only
+// the last row tile's epilogue is on the critical path.
 // Barriers (all waits bounded):
-//   zfull[kt]  generator -> MMA: K tile kt of the next tile is written
-//              (its arrival for kt = 0 also publishes the tile index and item)
-//   zempty[kt] MMA -> generator: the MMAs that read K tile kt are complete
-//   full/empty L-tile ring as before; tfull: all MMAs of the tile complete
-//   slot_free[s] epilogue -> generator: the tile in slot s is finished, its
-//              item slot may be reused
-// Per-K-tile use counts (the same on both sides) give the mbarrier parities,
-// since items of a batch have different numbers of K tiles.
+//   tile_pub[s]  generator -> other roles: tile index and item of slot s
+//   zfull[z]     generator -> MMA: the K tile in slot z written (one arrival
+//                per generator thread)
+//   zempty[z]    MMA -> generator: the MMAs that read slot z are complete
+//   full/empty   Lhat ring between producer and MMA issuer
+//   acc_full[m]  MMA -> epilogue: row tile m of the tile accumulated
+//   acc_free[m]  epilogue -> MMA: row tile m read (one arrival per warp)
+//   slot_free[s] epilogue -> generator: the tile in slot s is finished
+// The K-tile number g, use counts per row tile and per item slot (the same
+// on both sides of each barrier) give the phase parities, since items of a
+// batch differ in size.  The tile index is read after tile_pub, never after zfull[0]: slot s
+// is republished only after the epilogue finished the tile that used it, so
+// no waiter can fall a whole phase behind.
 static constexpr int kWsThreads = 1024;
-static constexpr int kWsTmemThreads = 128;
-static constexpr int kWsGenThreads = kWsThreads - kWsTmemThreads;
+static constexpr int kWsEpiWarps = 4;
+static constexpr int kWsMmaWarp = 4;
+static constexpr int kWsProdWarp = 5;
+static constexpr int kWsGenWarp0 = 6;
+static constexpr int kWsGenThreads = kWsThreads - 32 * kWsGenWarp0;
+static constexpr int kTcMaxMt = (kTcMaxKt * kTcKt + 1 + kTcRows - 1) / kTcRows;
+static constexpr int kWsZSlots = 4;  // K-tile slots of Z (hi + lo, 16 KB each)
+static constexpr int kWsStages = 5;  // Lhat ring stages (hi + lo, 32 KB each)
 
 __device__ __forceinline__ void named_sync(int id, int n)
 {
@@ -523,6 +592,13 @@ __device__ __forceinline__ int named_sync_or(int id, int n, int pred)
     return r;
 }
 
+// K tiles that row tile mt needs (lower triangle; the last row tile also
+// holds the portfolio row w^T L, which spans every column)
+__device__ __forceinline__ int tc_kts(int mt, int n_mt, int n_kt)
+{
+    return (mt == n_mt - 1) ? n_kt : min(n_kt, (kTcRows * (mt + 1) + kTcKt - 1) / kTcKt);
+}
+
 template <bool VAR, bool BATCH>
 __global__ void __launch_bounds__(kWsThreads, 1) mc_tcws_kernel(const __grid_constant__ TcBatch b)
 {
@@ -530,17 +606,18 @@ __global__ void __launch_bounds__(kWsThreads, 1) mc_tcws_kernel(const __grid_con
     const PlainArgs &a = b.var;
     unsigned char *base = (unsigned char *)(((uintptr_t)tc_smem + 1023) & ~(uintptr_t)1023);
     unsigned char *zhi = base;
-    unsigned char *zlo = zhi + b.n_kt_max * kTcZBytes;
-    unsigned char *lst = zlo + b.n_kt_max * kTcZBytes;
+    unsigned char *zlo = zhi + kWsZSlots * kTcZBytes;
+    unsigned char *lst = zlo + kWsZSlots * kTcZBytes;
 
-    __shared__ __align__(8) uint64_t full_bar[kTcStages], empty_bar[kTcStages], tfull_bar;
-    __shared__ __align__(8) uint64_t zfull[kTcMaxKt], zempty[kTcMaxKt], slot_free[2];
+    __shared__ __align__(8) uint64_t full_bar[kWsStages], empty_bar[kWsStages];
+    __shared__ __align__(8) uint64_t zfull[kWsZSlots], zempty[kWsZSlots];
+    __shared__ __align__(8) uint64_t acc_full[kTcMaxMt], acc_free[kTcMaxMt];
+    __shared__ __align__(8) uint64_t tile_pub[2], slot_free[2], drain_bar;
     __shared__ uint32_t tmem_base_sh;
     __shared__ int sS[kTcPaths];
     __shared__ float sPort[kTcPaths];
-    // abort flag of the tensor-memory side: written by its threads before a
-    // group barrier and read after it, so every decision taken on it is
-    // uniform across the group (the generator only skips waits on it)
+    // set by a role whose bounded wait ran out; the others then make no
+    // further waits and finish
     __shared__ int tm_abort;
     __shared__ long long s_tile[2];
     __shared__ long long s_unit;
@@ -555,17 +632,23 @@ __global__ void __launch_bounds__(kWsThreads, 1) mc_tcws_kernel(const __grid_con
         sPort[tid] = 0.f;
     }
     if (tid == 0) {
-        for (int s = 0; s < kTcStages; s++) {
+        for (int s = 0; s < kWsStages; s++) {
             mbar_init(&full_bar[s], 1);
             mbar_init(&empty_bar[s], 1);
         }
-        for (int k = 0; k < kTcMaxKt; k++) {
-            mbar_init(&zfull[k], kWsGenThreads); // every generator thread arrives once per tile
-            mbar_init(&zempty[k], 1);
+        for (int z = 0; z < kWsZSlots; z++) {
+            mbar_init(&zfull[z], kWsGenThreads);
+            mbar_init(&zempty[z], 1);
         }
-        mbar_init(&slot_free[0], 1);
-        mbar_init(&slot_free[1], 1);
-        mbar_init(&tfull_bar, 1);
+        for (int m = 0; m < kTcMaxMt; m++) {
+            mbar_init(&acc_full[m], 1);
+            mbar_init(&acc_free[m], kWsEpiWarps);
+        }
+        for (int s = 0; s < 2; s++) {
+            mbar_init(&tile_pub[s], 1);
+            mbar_init(&slot_free[s], 1);
+        }
+        mbar_init(&drain_bar, 1);
         tm_abort = 0;
         asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
     }
@@ -580,25 +663,23 @@ __global__ void __launch_bounds__(kWsThreads, 1) mc_tcws_kernel(const __grid_con
     const uint32_t tmem = tmem_base_sh;
     const long long total = b.dyn ? b.dyn[1] : b.total_tiles;
     const int n_items = b.dyn ? (int)b.dyn[0] : b.n_items;
-    // bit kt = parity of the number of tiles so far that used K tile kt (the
-    // same on both sides; it selects the mbarrier phase to wait for)
-    unsigned zpar = 0;
     int n_tail = 0;
     long long tail_fx = 0;
 
-    if (warp >= kWsTmemThreads / 32) {
+    if (warp >= kWsGenWarp0) {
         // ======================= generator =======================
-        // gab: this thread's abort flag. Threads of the group do not meet at
-        // K-tile boundaries, so a timeout is first local; the reduction barrier
-        // at the start of each tile makes it uniform before any decision that
-        // changes barrier participation.
-        const int gtid = tid - kWsTmemThreads;
+        // gab: this thread's abort flag.  Generator threads do not meet at
+        // K-tile boundaries, so a timeout is first local; the reduction
+        // barrier at the start of each tile makes it uniform before any
+        // decision that changes barrier participation.
+        const int gtid = tid - 32 * kWsGenWarp0;
+        unsigned g0 = 0; // K tiles of the previous path tiles
         int gab = 0;
         long long unit = -1, unit_end = 0, next_static = blockIdx.x;
         for (unsigned j = 0;; j++) {
             const int slot = j & 1;
-            // the item slot must be free (epilogue of tile j-2 done); after an
-            // abort on either side no wait is made (only barrier order is kept)
+            // the slot must be free (epilogue of tile j-2 done); after an
+            // abort on either side no wait is made
             if (!gab && !tm_abort && !mbar_wait(&slot_free[slot], ((j >> 1) & 1u) ^ 1u)) {
                 atomicOr(b.err, 8u);
                 gab = 1;
@@ -639,12 +720,9 @@ __global__ void __launch_bounds__(kWsThreads, 1) mc_tcws_kernel(const __grid_con
                 for (int w = gtid; w < (int)(sizeof(TcItem) / 4); w += kWsGenThreads) dst[w] = src[w];
                 named_sync(2, kWsGenThreads);
             }
-            if (tile < 0) { // uniform: gtid 0 publishes -1 after any abort
-                // publish the end (after the MMA side consumed K tile 0 of the last tile)
-                if (!gab && !tm_abort && !mbar_wait(&zempty[0], (zpar & 1u) ^ 1u)) gab = 1;
-                mbar_arrive(&zfull[0]); // every generator thread: completes the phase
-                break;
-            }
+            // publish the tile (or the end, -1) to the other roles
+            if (gtid == 0) mbar_arrive(&tile_pub[slot]);
+            if (tile < 0) break; // uniform: every thread read the same s_tile
             const TcItem &it = BATCH ? s_item[slot] : b.one;
             const int n = it.n, nq = (n + 3) >> 2, n_kt = it.n_kt;
             const long long p0 = (tile - it.tile_begin) * kTcPaths;
@@ -652,8 +730,10 @@ __global__ void __launch_bounds__(kWsThreads, 1) mc_tcws_kernel(const __grid_con
             // arrives on zfull[kt] once it has written its share of kt (no
             // group barrier, so no thread idles at K-tile boundaries)
             for (int kt = 0; kt < n_kt; kt++) {
-                // the previous tile's MMAs on this K tile are done
-                if (!gab && !tm_abort && !mbar_wait(&zempty[kt], ((zpar >> kt) & 1u) ^ 1u)) {
+                const unsigned g = g0 + (unsigned)kt;
+                const int zs = (int)(g % kWsZSlots);
+                // the MMAs on the slot's previous K tile (g - kWsZSlots) are done
+                if (!gab && !tm_abort && !mbar_wait(&zempty[zs], ((g / kWsZSlots) & 1u) ^ 1u)) {
                     atomicOr(b.err, 16u);
                     gab = 1;
                 }
@@ -684,47 +764,43 @@ __global__ void __launch_bounds__(kWsThreads, 1) mc_tcws_kernel(const __grid_con
                     }
                     unsigned short h[4], l[4];
                     for (int e = 0; e < 4; e++) split2(z[e], it.bf16, h[e], l[e]);
-                    const uint32_t off = (uint32_t)kt * kTcZBytes + sw128_offset(p, 4 * (item >> 6));
+                    const uint32_t off = (uint32_t)zs * kTcZBytes + sw128_offset(p, 4 * (item >> 6));
                     *reinterpret_cast<uint2 *>(zhi + off) =
                         make_uint2((uint32_t)h[0] | ((uint32_t)h[1] << 16), (uint32_t)h[2] | ((uint32_t)h[3] << 16));
                     *reinterpret_cast<uint2 *>(zlo + off) =
                         make_uint2((uint32_t)l[0] | ((uint32_t)l[1] << 16), (uint32_t)l[2] | ((uint32_t)l[3] << 16));
                 }
                 fence_async_shared(); // this thread's writes -> async proxy (tensor cores)
-                mbar_arrive(&zfull[kt]);
-                zpar ^= 1u << kt;
+                mbar_arrive(&zfull[zs]);
             }
+            g0 += (unsigned)n_kt;
         }
-    } else {
-        // ======================= tensor-memory side =======================
-        unsigned prod_iter = 0, cons_iter = 0;
-        for (unsigned j = 0;; j++) {
-            const int slot = j & 1;
-            // K tile 0 of tile j is written and its index published
-            if (!mbar_wait(&zfull[0], zpar & 1u)) {
-                atomicOr(b.err, 32u);
-                tm_abort = 1;
-            }
-            named_sync(1, kWsTmemThreads);
-            const long long tile = s_tile[slot];
-            if (tile < 0 || tm_abort) break; // uniform: both read after the group barrier
-            const TcItem &it = BATCH ? s_item[slot] : b.one;
-            const int n = it.n, n_kt = it.n_kt, n_mt = it.n_mt;
-            tc_fence_after();
-            if (warp == 1 && lane == 0) {
-                // producer: Lhat tiles in (K tile, row tile) order
+    } else if (warp == kWsProdWarp) {
+        // ======================= Lhat producer =======================
+        if (lane == 0) {
+            unsigned prod_iter = 0;
+            int skipped = -1; // the stage left unfilled by the fault injection
+            for (unsigned j = 0; !tm_abort; j++) {
+                const int slot = j & 1;
+                if (!mbar_wait(&tile_pub[slot], (j >> 1) & 1u)) {
+                    atomicOr(b.err, 32u);
+                    tm_abort = 1;
+                    break;
+                }
+                if (s_tile[slot] < 0) break;
+                const TcItem &it = BATCH ? s_item[slot] : b.one;
+                const int n_kt = it.n_kt, n_mt = it.n_mt;
                 for (int kt = 0; kt < n_kt && !tm_abort; kt++) {
                     for (int mt = 0; mt < n_mt; mt++) {
-                        const int kts = (mt == n_mt - 1) ? n_kt : min(n_kt, (kTcRows * (mt + 1) + kTcKt - 1) / kTcKt);
-                        if (kt >= kts) continue;
-                        const int s = prod_iter % kTcStages;
-                        if (!mbar_wait(&empty_bar[s], ((prod_iter / kTcStages) & 1u) ^ 1u)) {
+                        if (kt >= tc_kts(mt, n_mt, n_kt)) continue;
+                        const int s = prod_iter % kWsStages;
+                        if (tm_abort || !mbar_wait(&empty_bar[s], ((prod_iter / kWsStages) & 1u) ^ 1u)) {
                             atomicOr(b.err, 1u);
                             tm_abort = 1;
                             break;
                         }
                         if (b.inject_stall && prod_iter == 1) { // never filled: the consumer's wait runs out
-                            prod_iter++;
+                            skipped = (int)prod_iter++;
                             continue;
                         }
                         mbar_expect_tx(&full_bar[s], 2 * kTcTileBytes);
@@ -735,96 +811,144 @@ __global__ void __launch_bounds__(kWsThreads, 1) mc_tcws_kernel(const __grid_con
                         prod_iter++;
                     }
                 }
-            } else if (warp == 0 && lane == 0) {
-                // MMA issuer, K-tile-outer
+            }
+            // the copies still in flight land before the kernel ends
+            for (unsigned i = prod_iter > kWsStages ? prod_iter - kWsStages : 0; i < prod_iter; i++)
+                if ((int)i != skipped) mbar_wait(&full_bar[i % kWsStages], (i / kWsStages) & 1u);
+        }
+        __syncwarp();
+    } else if (warp == kWsMmaWarp) {
+        // ======================= MMA issuer =======================
+        if (lane == 0) {
+            unsigned g0 = 0, fpar = 0; // fpar bit m: parity of the uses of row tile m
+            unsigned rs = 0, rph = 0;  // Lhat ring: stage and phase parity of the next pair
+            const uint32_t lst_lo = sw128_desc_lo(smem_u32(lst));
+            for (unsigned j = 0; !tm_abort; j++) {
+                const int slot = j & 1;
+                if (!mbar_wait(&tile_pub[slot], (j >> 1) & 1u)) {
+                    atomicOr(b.err, 32u);
+                    tm_abort = 1;
+                    break;
+                }
+                if (s_tile[slot] < 0) break;
+                const TcItem &it = BATCH ? s_item[slot] : b.one;
+                const int n_kt = it.n_kt, n_mt = it.n_mt;
                 const uint32_t idesc = tc_idesc(it.bf16, kTcRows, kTcPaths);
                 for (int kt = 0; kt < n_kt && !tm_abort; kt++) {
-                    if (kt > 0 && !mbar_wait(&zfull[kt], (zpar >> kt) & 1u)) {
+                    const unsigned g = g0 + (unsigned)kt;
+                    const int zs = (int)(g % kWsZSlots);
+                    if (!mbar_wait(&zfull[zs], (g / kWsZSlots) & 1u)) {
                         atomicOr(b.err, 64u);
                         tm_abort = 1;
                         break;
                     }
                     tc_fence_after();
-                    const uint32_t zh = smem_u32(zhi + (size_t)kt * kTcZBytes);
-                    const uint32_t zl = smem_u32(zlo + (size_t)kt * kTcZBytes);
+                    const uint32_t zh_lo = sw128_desc_lo(smem_u32(zhi + (size_t)zs * kTcZBytes));
+                    const uint32_t zl_lo = sw128_desc_lo(smem_u32(zlo + (size_t)zs * kTcZBytes));
                     for (int mt = 0; mt < n_mt; mt++) {
-                        const int kts = (mt == n_mt - 1) ? n_kt : min(n_kt, (kTcRows * (mt + 1) + kTcKt - 1) / kTcKt);
+                        const int kts = tc_kts(mt, n_mt, n_kt);
                         if (kt >= kts) continue;
-                        const int s = cons_iter % kTcStages;
-                        if (!mbar_wait(&full_bar[s], (cons_iter / kTcStages) & 1u)) {
+                        // the first write to row tile mt: the epilogue has read the previous tile's
+                        if (kt == 0 && !mbar_wait(&acc_free[mt], ((fpar >> mt) & 1u) ^ 1u)) {
+                            atomicOr(b.err, 128u);
+                            tm_abort = 1;
+                            break;
+                        }
+                        if (!mbar_wait(&full_bar[rs], rph)) {
                             atomicOr(b.err, 2u);
                             tm_abort = 1;
                             break;
                         }
                         tc_fence_after();
-                        const uint32_t lhi = smem_u32(lst + (size_t)s * 2 * kTcTileBytes);
-                        const uint32_t llo = lhi + kTcTileBytes;
-                        const uint32_t d_tmem = tmem + (uint32_t)(mt * kTcPaths);
-#pragma unroll
-                        for (int ks = 0; ks < kTcKt / 16; ks++) {
-                            const uint32_t o = (uint32_t)ks * 32;
-                            const uint32_t acc0 = (kt > 0 || ks > 0) ? 1u : 0u;
-                            tc_mma(d_tmem, sw128_desc(lhi + o), sw128_desc(zh + o), idesc, acc0);
-                            tc_mma(d_tmem, sw128_desc(lhi + o), sw128_desc(zl + o), idesc, 1u);
-                            tc_mma(d_tmem, sw128_desc(llo + o), sw128_desc(zh + o), idesc, 1u);
+                        tc_mma_pair(tmem + (uint32_t)(mt * kTcPaths), lst_lo + (uint32_t)rs * (2 * kTcTileBytes >> 4),
+                                    zh_lo, zl_lo, idesc, kt > 0 ? 1u : 0u);
+                        tc_commit(&empty_bar[rs]);
+                        if (++rs == kWsStages) {
+                            rs = 0;
+                            rph ^= 1u;
                         }
-                        tc_commit(&empty_bar[s]);
-                        cons_iter++;
+                        if (kt == kts - 1) tc_commit(&acc_full[mt]); // row tile mt complete
                     }
-                    tc_commit(&zempty[kt]); // K tile kt may be overwritten once these MMAs complete
+                    tc_commit(&zempty[zs]); // the slot may be overwritten once these MMAs complete
                 }
-                tc_commit(&tfull_bar);
+                g0 += (unsigned)n_kt;
+                fpar ^= (1u << n_mt) - 1u;
             }
-            // lanes 1-31 of warps 0 and 1 wait here, blocked, for their lane 0
-            // (the producer and the MMA issuer): spinning on tfull_bar beside
-            // it would take its issue slots
-            __syncwarp();
-            // per-K-tile use parities advance on this side too
-            zpar ^= (1u << n_kt) - 1u;
-            // ---- epilogue (warps 0-3)
-            if (!mbar_wait(&tfull_bar, j & 1u)) {
-                atomicOr(b.err, 4u);
+            // every MMA issued (and every commit's arrival) completes before
+            // the tensor memory and the barriers are released
+            tc_commit(&drain_bar);
+            mbar_wait(&drain_bar, 0u);
+        }
+        __syncwarp();
+    } else {
+        // ======================= epilogue (warps 0-3) =======================
+        unsigned apar = 0; // bit m: parity of the uses of row tile m
+        for (unsigned j = 0;; j++) {
+            const int slot = j & 1;
+            int ab = 0;
+            if (!tm_abort && !mbar_wait(&tile_pub[slot], (j >> 1) & 1u)) {
+                atomicOr(b.err, 32u);
+                ab = 1;
+            }
+            if (named_sync_or(1, 32 * kWsEpiWarps, ab || tm_abort)) { // uniform over the four warps
                 tm_abort = 1;
+                break;
             }
-            tc_fence_after();
-            named_sync(1, kWsTmemThreads);
-            if (!tm_abort) {
-                const int quarter = warp; // lanes 32*warp .. +31
-                for (int mt = 0; mt < n_mt; mt++) {
-                    const int row = mt * kTcRows + quarter * 32 + lane;
-                    const bool asset = row < n;
-                    const float thr = asset ? (float)(((double)it.neg_x - (double)it.horizon * it.mu64[row]) * kTcLScale)
-                                            : 0.f;
+            const long long tile = s_tile[slot];
+            if (tile < 0) break;
+            const TcItem &it = BATCH ? s_item[slot] : b.one;
+            const int n = it.n, n_mt = it.n_mt;
+            bool dead = false;
+            for (int mt = 0; mt < n_mt; mt++) {
+                int wab = 0;
+                if (!tm_abort && !mbar_wait(&acc_full[mt], (apar >> mt) & 1u)) {
+                    atomicOr(b.err, 4u);
+                    wab = 1;
+                }
+                if (named_sync_or(1, 32 * kWsEpiWarps, wab || tm_abort)) {
+                    dead = true;
+                    break;
+                }
+                tc_fence_after();
+                const int row = mt * kTcRows + warp * 32 + lane;
+                const bool asset = row < n;
+                const float thr = asset ? tc_threshold(it, row) : 0.f;
 #pragma unroll
-                    for (int cb = 0; cb < kTcPaths / 16; cb++) {
-                        const uint32_t taddr = tmem + ((uint32_t)(quarter * 32) << 16) + (uint32_t)(mt * kTcPaths + cb * 16);
-                        uint32_t v[16];
-                        asm volatile("tcgen05.ld.sync.aligned.32x32b.x16.b32 "
-                                     "{%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, [%16];"
-                                     : "=r"(v[0]), "=r"(v[1]), "=r"(v[2]), "=r"(v[3]), "=r"(v[4]), "=r"(v[5]),
-                                       "=r"(v[6]), "=r"(v[7]), "=r"(v[8]), "=r"(v[9]), "=r"(v[10]), "=r"(v[11]),
-                                       "=r"(v[12]), "=r"(v[13]), "=r"(v[14]), "=r"(v[15])
-                                     : "r"(taddr));
-                        asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
-                        int cnt = 0;
+                for (int cb = 0; cb < kTcPaths / 16; cb++) {
+                    const uint32_t taddr = tmem + ((uint32_t)(warp * 32) << 16) + (uint32_t)(mt * kTcPaths + cb * 16);
+                    uint32_t v[16];
+                    asm volatile("tcgen05.ld.sync.aligned.32x32b.x16.b32 "
+                                 "{%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, [%16];"
+                                 : "=r"(v[0]), "=r"(v[1]), "=r"(v[2]), "=r"(v[3]), "=r"(v[4]), "=r"(v[5]),
+                                   "=r"(v[6]), "=r"(v[7]), "=r"(v[8]), "=r"(v[9]), "=r"(v[10]), "=r"(v[11]),
+                                   "=r"(v[12]), "=r"(v[13]), "=r"(v[14]), "=r"(v[15])
+                                 : "r"(taddr));
+                    asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+                    int cnt = 0;
 #pragma unroll
-                        for (int c = 0; c < 16; c++) {
-                            const unsigned m = __ballot_sync(0xffffffffu, asset && __uint_as_float(v[c]) < thr);
-                            if (lane == c) cnt = __popc(m);
-                        }
-                        if (lane < 16 && cnt) atomicAdd(&sS[cb * 16 + lane], cnt);
-                        if (row == n) {
+                    for (int c = 0; c < 16; c++) {
+                        const unsigned m = __ballot_sync(0xffffffffu, asset && __uint_as_float(v[c]) < thr);
+                        if (lane == c) cnt = __popc(m);
+                    }
+                    if (lane < 16 && cnt) atomicAdd(&sS[cb * 16 + lane], cnt);
+                    if (row == n) {
 #pragma unroll
-                            for (int c = 0; c < 16; c++)
-                                sPort[cb * 16 + c] =
-                                    (float)(it.hwmu + (double)(__uint_as_float(v[c]) * (1.0f / kTcLScale)));
-                        }
+                        for (int c = 0; c < 16; c++)
+                            sPort[cb * 16 + c] = it.hwmu_f + __uint_as_float(v[c]) * (1.0f / kTcLScale);
                     }
                 }
+                // this warp's reads of row tile mt are complete: the next tile may overwrite it
+                tc_fence_before();
+                __syncwarp();
+                if (lane == 0) mbar_arrive(&acc_free[mt]);
             }
-            tc_fence_before();
-            named_sync(1, kWsTmemThreads);
-            if (!tm_abort && tid < kTcPaths) {
+            if (dead) {
+                tm_abort = 1;
+                break;
+            }
+            apar ^= (1u << n_mt) - 1u;
+            named_sync(1, 32 * kWsEpiWarps); // every count of the tile is in sS / sPort
+            if (tid < kTcPaths) {
                 const long long p = (tile - it.tile_begin) * kTcPaths + tid;
                 int crash = 0, breach = 0;
                 if (p < it.n_paths) {
@@ -842,25 +966,11 @@ __global__ void __launch_bounds__(kWsThreads, 1) mc_tcws_kernel(const __grid_con
                     if (crash) atomicAdd(&it.counts[0], (unsigned long long)crash);
                     if (breach) atomicAdd(&it.counts[1], (unsigned long long)breach);
                 }
-            }
-            if (tid < kTcPaths) {
                 sS[tid] = 0;
                 sPort[tid] = 0.f;
             }
-            named_sync(1, kWsTmemThreads);
-            tc_fence_after();
-            if (tid == 0) mbar_arrive(&slot_free[slot]); // the generator may reuse this item slot
-        }
-        // drain on abort: MMAs and copies issued but not waited for
-        if (tm_abort) {
-            if (warp == 0 && lane == 0) {
-                tc_commit(&tfull_bar);
-                mbar_wait(&tfull_bar, 0u);
-                mbar_wait(&tfull_bar, 1u);
-            }
-            if (warp == 1 && lane == 0)
-                for (unsigned i = cons_iter; i < prod_iter; i++)
-                    mbar_wait(&full_bar[i % kTcStages], (i / kTcStages) & 1u);
+            named_sync(1, 32 * kWsEpiWarps); // resets done before the next tile's counts
+            if (tid == 0) mbar_arrive(&slot_free[slot]); // the generator may reuse this slot
         }
     }
     tc_fence_before();
@@ -928,6 +1038,11 @@ static int tmem_cols_for(int n_mt)
     return c;
 }
 
+static size_t ws_smem_bytes()
+{
+    return 1024 + (size_t)kWsZSlots * 2 * kTcZBytes + (size_t)kWsStages * 2 * kTcTileBytes;
+}
+
 static size_t tc_smem_bytes(int n_kt_max)
 {
     return 1024 + (size_t)n_kt_max * 2 * kTcZBytes + (size_t)kTcStages * 2 * kTcTileBytes;
@@ -947,6 +1062,7 @@ static void fill_item(TcItem &it, const PlainArgs &a, const unsigned char *tiles
     it.tile_begin = tile_begin;
     it.keys = a.keys;
     it.hwmu = (double)a.horizon * wmu;
+    it.hwmu_f = (float)it.hwmu;
     it.n = a.n;
     it.n_mt = tc_row_tiles(a.n);
     it.n_kt = tc_k_tiles(a.n);
@@ -978,18 +1094,17 @@ cudaError_t launch_tc(const PlainArgs &a, const unsigned char *tiles, int bf16, 
     b.tmem_cols = tmem_cols_for(b.one.n_mt);
     b.var = a;
     if (b.one.n_mt * kTcPaths > 512) return cudaErrorInvalidValue;
-    const size_t smem = tc_smem_bytes(b.n_kt_max);
-    // Daily draws: the warp-specialised kernel (generation, which dominates,
-    // overlaps the MMAs and the epilogue).  Aggregated draws: generation is
-    // cheap and the single TMEM accumulator serialises MMAs and epilogue, so
-    // the phase-serial kernel, whose epilogue runs on all 16 warps, is faster.
-    // RG_TC_KERNEL=simple|ws overrides the choice.
+    // The warp-specialised kernel: generation, MMAs and the per-row-tile
+    // epilogue overlap.  RG_TC_KERNEL=simple selects the phase-serial kernel
+    // (generate, multiply, read back in turn), kept as a second
+    // implementation that the tests compare.
     const char *sel = getenv("RG_TC_KERNEL");
-    bool simple = aggregated;
+    bool simple = false;
     if (sel && strstr(sel, "simple")) simple = true;
     if (sel && strstr(sel, "ws")) simple = false;
     auto kern = simple ? ((a.var_mode != 0) ? mc_tc_kernel<true, false> : mc_tc_kernel<false, false>)
                        : ((a.var_mode != 0) ? mc_tcws_kernel<true, false> : mc_tcws_kernel<false, false>);
+    const size_t smem = simple ? tc_smem_bytes(b.n_kt_max) : ws_smem_bytes();
     cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess) return e;
     long long grid = sm_count;
@@ -1028,18 +1143,19 @@ cudaError_t launch_tc_batch(const void *d_items, int n_items, long long total_ti
     b.n_kt_max = n_kt_max;
     b.tmem_cols = tmem_cols_for(n_mt_max);
     if (n_mt_max * kTcPaths > 512 || n_kt_max > kTcMaxKt) return cudaErrorInvalidValue;
-    const size_t smem = tc_smem_bytes(n_kt_max);
-    mc_tcws_kernel<false, true><<<(unsigned)grid, kWsThreads, smem, s>>>(b);
+    mc_tcws_kernel<false, true><<<(unsigned)grid, kWsThreads, ws_smem_bytes(), s>>>(b);
     return cudaGetLastError();
 }
 
-// Resident CTAs per SM of the batched kernel for this largest item
-// (registers and shared memory; tensor memory is checked by the caller).
+// Resident CTAs per SM of the batched kernel (registers and shared memory,
+// which the warp-specialised kernel sizes independently of the items;
+// tensor memory is checked by the caller).
 int tc_batch_occupancy(int n_kt_max)
 {
+    (void)n_kt_max;
     int per_sm = 0;
     if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, mc_tcws_kernel<false, true>, kWsThreads,
-                                                      tc_smem_bytes(n_kt_max)) != cudaSuccess)
+                                                      ws_smem_bytes()) != cudaSuccess)
         return 1;
     return per_sm < 1 ? 1 : per_sm;
 }
@@ -1049,7 +1165,7 @@ int tc_batch_occupancy(int n_kt_max)
 cudaError_t tc_batch_prepare()
 {
     return cudaFuncSetAttribute(mc_tcws_kernel<false, true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                (int)tc_smem_bytes(kTcMaxKt));
+                                (int)ws_smem_bytes());
 }
 
 } // namespace rg

@@ -36,9 +36,8 @@ def _case(n, seed):
     return mu, sigma, w
 
 
-# the two tcgen05 kernels: "ws" (warp-specialised, chosen for daily draws)
-# and "simple" (phase-serial, chosen for aggregated draws); RG_TC_KERNEL
-# forces one of them
+# the two tcgen05 kernels: "ws" (warp-specialised, the default) and "simple"
+# (phase-serial); RG_TC_KERNEL forces one of them
 KERNELS = ["ws", "simple"]
 
 
