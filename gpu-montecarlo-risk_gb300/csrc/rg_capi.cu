@@ -389,7 +389,7 @@ int rg_portfolio_create(int32_t n, const double *mu, const double *sigma, int64_
         RG_CUDA_TRY(cudaMalloc(&p->d_tc[1], tc_tile_bytes(n)));
     }
     RG_CUDA_TRY(cudaMalloc(&p->d_w32, (size_t)n * sizeof(float)));
-    RG_CUDA_TRY(cudaMalloc(&p->d_aux, 2 * sizeof(double)));
+    RG_CUDA_TRY(cudaMalloc(&p->d_aux, (2 + 2 * (size_t)n) * sizeof(double))); // moments + factorisation scratch
     RG_CUDA_TRY(cudaMalloc(&p->d_info, sizeof(int)));
     if (!dev_in) {
         RG_CUDA_TRY(cudaMalloc(&dA, nn * sizeof(double)));

@@ -118,7 +118,7 @@ struct Portfolio {
     unsigned char *d_tc[2] = {nullptr, nullptr}; // tensor-core tiles (FP16, BF16), N <= tc_max_n()
     unsigned int *d_err = nullptr; // error word of the tensor-core kernel
     float *d_w32 = nullptr;    // n (zeros when no weights)
-    double *d_aux = nullptr;   // [2]: w^T Sigma w, w.mu
+    double *d_aux = nullptr;   // [2 + 2n]: w^T Sigma w, w.mu, then factorisation scratch
     int *d_info = nullptr;
     double wsw = 0.0, wmu = 0.0;
     float ms_chol = 0.f;

@@ -44,8 +44,14 @@ def _assert_S_parity(S_gpu, S_ref, R_ref, x, max_near_frac=1e-2):
     return int(near.sum())
 
 
-@pytest.mark.parametrize("n", [1, 3, 16, 20, 33, 50, 63, 64])
-def test_cholesky_matches_oracle(gpu, oracle, n):
+@pytest.mark.parametrize("form,n", [("auto", n) for n in (1, 3, 16, 20, 33, 50, 63, 64, 65, 130, 600)]
+                         + [("blocked", n) for n in (1, 3, 31, 32, 33, 64)] + [("single", 130)])
+def test_cholesky_matches_oracle(gpu, oracle, monkeypatch, form, n):
+    """Single-CTA form up to N = 64, blocked multi-SM form above (and either
+    forced by RG_CHOLESKY): L within 1e-12 of the oracle, moments exact to
+    rounding."""
+    if form != "auto":
+        monkeypatch.setenv("RG_CHOLESKY", form)
     from riskgpu import synth
     rng = np.random.default_rng(n)
     mu, sigma, _, _ = synth.one_factor_sigma(rng, n)
@@ -58,6 +64,26 @@ def test_cholesky_matches_oracle(gpu, oracle, n):
     w = np.full(n, 1.0 / n)
     assert abs(inf["wsw"] - w @ sigma @ w) <= 1e-15 + 1e-12 * abs(w @ sigma @ w)
     assert abs(inf["wmu"] - w @ mu) <= 1e-15
+
+
+@pytest.mark.parametrize("form", ["single", "blocked"])
+def test_cholesky_errors_at_a_later_pivot(gpu, monkeypatch, form):
+    """A matrix that fails at column 70 (inside the third block of the
+    blocked form), and a NaN in the lower triangle, give the same errors in
+    both forms."""
+    monkeypatch.setenv("RG_CHOLESKY", form)
+    n = 100
+    a = np.eye(n) * 2.0
+    a[70, 70] = -1.0
+    with pytest.raises(gpu.RiskGpuError) as e:
+        gpu.Portfolio(np.zeros(n), a)
+    assert e.value.status == gpu.RG_ERR_NOT_PD
+    assert "pivot 70" in str(e.value)
+    a = np.eye(n)
+    a[80, 3] = np.nan
+    with pytest.raises(gpu.RiskGpuError) as e:
+        gpu.Portfolio(np.zeros(n), a)
+    assert e.value.status == gpu.RG_ERR_INVALID
 
 
 def test_cholesky_errors(gpu):
