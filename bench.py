@@ -372,7 +372,8 @@ def engine_arm(args):
 
     line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": ms_per_step, "higher_is_better": True,
-            "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+            "scaling": "weak", "vs_baseline": None,
+            "dtype": {"fp16x3": "f16x3", "bf16x3": "bf16x3"}.get(args.precision, "f32"), "data": "synthetic",
             "config": config(args, world, p),
             "e2e": {"value": world * args.paths / e2e_s, "unit": UNIT, "h2d_bytes_per_step": h2d,
                     "d2h_bytes_per_step": d2h, "ms_per_step": 1e3 * e2e_s, "path": e2e_path},

@@ -21,7 +21,7 @@
 // Above kCholSingleMaxN a blocked right-looking form spreads the work over
 // the SMs (one SM's FP64 rate is a small fraction of the part's): for each
 // 32-column block k,
-//   chol_diag    one warp factors the diagonal block in shared memory,
+//   chol_diag    one warp factors the diagonal block in registers,
 //   chol_panel   one thread per row solves L_ik L_kk^T = A_ik below it,
 //   chol_update  one CTA per 32 x 32 tile of the trailing lower triangle
 //                subtracts L_ik L_jk^T,
@@ -193,44 +193,55 @@ __global__ void chol_prep_kernel(const double *__restrict__ A, long long lda, in
 }
 
 // Factor the diagonal block at k0 (kb <= 32 columns) with one warp; lane r
-// owns row r of the block.
+// holds row r of the block in registers (fully unrolled), and column values
+// move between lanes by shuffles.  Right-looking: after column c is scaled,
+// lane r subtracts L_rc L_jc from its entries j in (c, r].
 __global__ void chol_diag_kernel(double *__restrict__ L, int n, int k0, int kb, int *__restrict__ info)
 {
     if (*info != 0) return;
-    __shared__ double a[kCholNb][kCholNb + 1];
     const int r = threadIdx.x;
-    for (int c = 0; c < kCholNb; c++)
-        a[r][c] = (r < kb && c <= r) ? L[(long long)(k0 + r) * n + k0 + c] : 0.0;
-    __syncwarp();
-    for (int c = 0; c < kb; c++) {
-        const double d = a[c][c]; // every lane reads the same value: the branch is uniform
-        if (!(d > 0.0) || !isfinite(d)) {
-            if (r == 0) *info = k0 + c + 1;
-            return;
+    double a[kCholNb];
+#pragma unroll
+    for (int c = 0; c < kCholNb; c++) a[c] = (r < kb && c <= r) ? L[(long long)(k0 + r) * n + k0 + c] : 0.0;
+#pragma unroll
+    for (int c = 0; c < kCholNb; c++) {
+        if (c < kb) {
+            const double d = __shfl_sync(0xffffffffu, a[c], c); // the same value in every lane: uniform branch
+            if (!(d > 0.0) || !isfinite(d)) {
+                if (r == 0) *info = k0 + c + 1;
+                return;
+            }
+            // one FP64 reciprocal square root per column instead of a square
+            // root and a division: both are long FP64 sequences on this part
+            const double rs = rsqrt(d);
+            if (r == c) a[c] = d * rs;
+            if (r > c) a[c] = a[c] * rs;
+#pragma unroll
+            for (int j = c + 1; j < kCholNb; j++) {
+                const double ljc = __shfl_sync(0xffffffffu, a[c], j);
+                if (r >= j) a[j] = fma(-a[c], ljc, a[j]);
+            }
         }
-        const double piv = sqrt(d);
-        __syncwarp();
-        if (r == c) a[c][c] = piv;
-        if (r > c && r < kb) a[r][c] = a[r][c] / piv;
-        __syncwarp();
-        if (r > c && r < kb) {
-            const double lrc = a[r][c];
-            for (int j = c + 1; j <= r; j++) a[r][j] = fma(-lrc, a[j][c], a[r][j]);
-        }
-        __syncwarp();
     }
-    if (r < kb)
-        for (int c = 0; c <= r; c++) L[(long long)(k0 + r) * n + k0 + c] = a[r][c];
+    if (r < kb) {
+#pragma unroll
+        for (int c = 0; c < kCholNb; c++)
+            if (c <= r) L[(long long)(k0 + r) * n + k0 + c] = a[c];
+    }
 }
 
-// Rows below the diagonal block: x L_kk^T = a, one thread per row (32 per CTA).
+// Rows below the diagonal block: x L_kk^T = a, one thread per row (32 per
+// CTA).  The dot products use four partial sums, so the dependent chain is a
+// quarter as long.
 __global__ void chol_panel_kernel(double *__restrict__ L, int n, int k0, int kb, const int *__restrict__ info)
 {
     if (*info != 0) return;
     __shared__ double lkk[kCholNb][kCholNb + 1];
+    __shared__ double inv[kCholNb];
     const int t = threadIdx.x;
     for (int c = 0; c < kCholNb; c++)
         lkk[t][c] = (t < kb && c <= t) ? L[(long long)(k0 + t) * n + k0 + c] : 0.0;
+    inv[t] = (t < kb) ? 1.0 / L[(long long)(k0 + t) * n + k0 + t] : 0.0; // one division per CTA lane
     __syncwarp();
     const int i = k0 + kb + blockIdx.x * kCholNb + t;
     if (i >= n) return;
@@ -239,10 +250,16 @@ __global__ void chol_panel_kernel(double *__restrict__ L, int n, int k0, int kb,
 #pragma unroll
     for (int c = 0; c < kCholNb; c++) {
         if (c < kb) {
-            double v = row[c];
+            double s0 = row[c], s1 = 0.0, s2 = 0.0, s3 = 0.0;
 #pragma unroll
-            for (int m = 0; m < c; m++) v = fma(-x[m], lkk[c][m], v);
-            x[c] = v / lkk[c][c];
+            for (int m = 0; m < c; m++) {
+                const double p = x[m] * lkk[c][m];
+                if ((m & 3) == 0) s0 -= p;
+                else if ((m & 3) == 1) s1 -= p;
+                else if ((m & 3) == 2) s2 -= p;
+                else s3 -= p;
+            }
+            x[c] = ((s0 + s1) + (s2 + s3)) * inv[c];
             row[c] = x[c];
         } else {
             x[c] = 0.0;
@@ -289,9 +306,11 @@ __global__ void chol_finish_kernel(const double *__restrict__ L, int n, float *_
 {
     __shared__ double red[33];
     if (*info != 0) return;
-    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+    // one warp per row
+    const int lane = threadIdx.x & 31, warps = (gridDim.x * blockDim.x) >> 5;
+    for (int i = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; i < n; i += warps) {
         const int off = packed_row_offset(i), len = 4 * (i / 4 + 1);
-        for (int j = 0; j < len; j++) Lp[off + j] = (j <= i) ? (float)L[(long long)i * n + j] : 0.f;
+        for (int j = lane; j < len; j += 32) Lp[off + j] = (j <= i) ? (float)L[(long long)i * n + j] : 0.f;
     }
     if (blockIdx.x == 0) {
         double a = 0.0, b = 0.0;
@@ -325,7 +344,7 @@ static cudaError_t launch_cholesky_blocked(const double *A, long long lda, int n
             chol_update_kernel<<<mb * (mb + 1) / 2, 256, 0, s>>>(L64, n, k0, kb, info);
         }
     }
-    chol_finish_kernel<<<(n + 255) / 256, 256, 0, s>>>(L64, n, Lp, aux, info);
+    chol_finish_kernel<<<(n + 7) / 8, 256, 0, s>>>(L64, n, Lp, aux, info);
     return cudaGetLastError();
 }
 
