@@ -44,7 +44,7 @@ EXPORTED_SYMBOLS = [
     "rg_batch_create", "rg_batch_launch", "rg_batch_wait", "rg_batch_info_get", "rg_batch_tune",
     "rg_batch_destroy", "rg_server_default_config", "rg_server_create", "rg_server_register",
     "rg_server_submit", "rg_server_wait", "rg_server_stats", "rg_server_reset_stats",
-    "rg_server_destroy",
+    "rg_server_destroy", "rg_moments", "rg_crash_frequency",
     "get_cuda_model", "cuda_simulate",
 ]
 
@@ -195,6 +195,11 @@ def lib():
         L.rg_server_reset_stats.argtypes = [ctypes.c_void_p]
         L.rg_server_destroy.argtypes = [ctypes.c_void_p]
         L.rg_probe_peaks.argtypes = [ctypes.POINTER(Peaks), ctypes.c_void_p]
+        L.rg_moments.argtypes = [ctypes.c_void_p, ctypes.c_int64, ctypes.c_int32, ctypes.c_int64,
+                                 ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p]
+        L.rg_crash_frequency.argtypes = [ctypes.c_void_p, ctypes.c_int64, ctypes.c_int32, ctypes.c_int64,
+                                         ctypes.c_double, ctypes.c_int32, ctypes.POINTER(ctypes.c_double),
+                                         ctypes.c_void_p]
         L.get_cuda_model.restype = ModelFunctions
         L.cuda_simulate.argtypes = [ctypes.POINTER(MonteCarloParams), ctypes.POINTER(MonteCarloResult)]
         _lib = L
@@ -397,6 +402,31 @@ def probe_peaks(stream=None) -> dict:
     pk = Peaks()
     check(lib().rg_probe_peaks(ctypes.byref(pk), stream))
     return {f: getattr(pk, f) for f, _ in pk._fields_}
+
+
+def moments(returns, stream=None):
+    """(mu, Sigma) of a T x N daily-returns matrix on the GPU (rg_moments):
+    column means and the ddof = 1 sample covariance, FP64."""
+    X = np.ascontiguousarray(returns, dtype=np.float64)
+    if X.ndim != 2:
+        raise ValueError("returns must be a 2-D array (days x indices)")
+    T, n = X.shape
+    mu = np.empty(n)
+    sigma = np.empty((n, n))
+    check(lib().rg_moments(X.ctypes.data, T, n, n, mu.ctypes.data, sigma.ctypes.data, stream))
+    return mu, sigma
+
+
+def crash_frequency(returns, x, k, stream=None) -> float:
+    """Fraction of days (rows) with at least k returns below -x, on the GPU
+    (rg_crash_frequency)."""
+    X = np.ascontiguousarray(returns, dtype=np.float64)
+    if X.ndim != 2:
+        raise ValueError("returns must be a 2-D array (days x indices)")
+    T, n = X.shape
+    out = ctypes.c_double()
+    check(lib().rg_crash_frequency(X.ctypes.data, T, n, n, float(x), int(k), ctypes.byref(out), stream))
+    return out.value
 
 
 def shard_range(rank: int, world: int, paths_per_rank: int):

@@ -249,6 +249,23 @@ int rg_server_destroy(rg_server *s);
  *  - `stream` NULL means the default stream; ms_device is left 0. */
 int rg_simulate_noalloc(const rg_portfolio *p, const rg_query *q, rg_result *out, void *stream);
 
+/* ---------------- preprocessing (daily returns -> mu, Sigma) ---------------- */
+/* Sample moments of a daily-returns matrix on the GPU, in FP64:
+ * mu_j = mean of column j; Sigma = sum_t (X_t - mu)(X_t - mu)^T / (T - 1)
+ * (ddof = 1), full symmetric, row-major n x n.  Replaces compute_stats
+ * (preprocessing/preprocessing_stats.py:18,21: pandas train.mean() and
+ * train.cov()).  `returns` is a T x n row-major HOST array with leading
+ * dimension ld >= n, T >= 2, every entry finite; mu_out (n) and sigma_out
+ * (n * n) are host arrays.  Synchronous on `stream` (NULL: default). */
+int rg_moments(const double *returns, int64_t T, int32_t n, int64_t ld, double *mu_out, double *sigma_out,
+               void *stream);
+
+/* Fraction of the T rows (days) on which at least k of the n returns are
+ * below -x.  Replaces compute_metrics (preprocessing/evaluation.py:19,22).
+ * Same array conventions as rg_moments (T >= 1). */
+int rg_crash_frequency(const double *returns, int64_t T, int32_t n, int64_t ld, double x, int32_t k,
+                       double *freq_out, void *stream);
+
 /* ---------------- measurement ---------------- */
 /* Roofline denominators of the fused kernels, measured on the current
  * device with micro-kernels timed by CUDA events on `stream`: FP32 FMA

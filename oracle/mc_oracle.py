@@ -15,7 +15,14 @@ Contents
     exactly N(H w.mu, H w^T Sigma w), so P(breach), VaR and CVaR are exact;
     for a one-factor covariance P(S >= k) is a one-dimensional integral over
     the market factor of a Poisson-binomial tail (Gauss-Hermite quadrature);
-  * the empirical VaR / CVaR definition the engine implements.
+  * the empirical VaR / CVaR definition the engine implements;
+  * the reference's preprocessing (preprocessing/fetch_split.py,
+    preprocessing_stats.py, evaluation.py) restated in plain Python loops
+    over dicts and lists: date alignment and split, two-pass column means and
+    ddof = 1 covariance, realised crash frequency.  Parity unpinned against
+    the reference's own output: its pandas code cannot run here (pandas is
+    not installed); these follow the documented definitions of
+    DataFrame.mean / DataFrame.cov and the reference's expressions.
 """
 from __future__ import annotations
 
@@ -326,3 +333,49 @@ def var_cvar(port_returns, alpha):
     part = np.partition(loss, M - T)
     tail = part[M - T:]
     return float(tail.min()), float(tail.mean()), T
+
+
+# ---------------------------------------------------------------- preprocessing
+def align_and_split(series, start, end, train_ratio):
+    """fetch_split.py:86-124 in plain Python: series maps name -> list of
+    (date, return) with datetime.date keys; returns (train_rows, test_rows),
+    each a list of (date, [returns in name order]).  Union of dates
+    ascending, [start, end] inclusive, rows with a missing (None / NaN)
+    return dropped, split at int(rows * train_ratio)."""
+    names = list(series.keys())
+    table = {}
+    for j, name in enumerate(names):
+        for d, r in series[name]:
+            table.setdefault(d, [None] * len(names))[j] = r
+    rows = []
+    for d in sorted(table):
+        if d < start or d > end:
+            continue
+        vals = table[d]
+        if any(v is None or v != v for v in vals):
+            continue
+        rows.append((d, vals))
+    split = int(len(rows) * train_ratio)
+    return rows[:split], rows[split:]
+
+
+def compute_stats(X):
+    """preprocessing_stats.py:18,21: column means and the ddof = 1 sample
+    covariance (two passes: means, then the sum of products of deviations),
+    in FP64; the means with math.fsum (correctly rounded)."""
+    X = np.asarray(X, dtype=np.float64)
+    T, n = X.shape
+    mu = np.array([math.fsum(X[:, j]) / T for j in range(n)])
+    D = X - mu
+    sigma = (D.T @ D) / (T - 1)
+    return mu, 0.5 * (sigma + sigma.T)
+
+
+def compute_metrics(X, x, k):
+    """evaluation.py:19,22: fraction of rows with at least k entries < -x."""
+    X = np.asarray(X, dtype=np.float64)
+    days = 0
+    for row in X:
+        if sum(1 for v in row if v < -x) >= k:
+            days += 1
+    return days / len(X)
