@@ -339,8 +339,31 @@ int64_t rg_tail_count(int64_t M, double level)
     return (int64_t)t;
 }
 
+// Optional device parts of a portfolio: the tiled kernel's L^T and the
+// tensor-core tiles (FP16 and BF16 splits).  A resident portfolio holds all
+// of them; the one-shot paths (rg_run, the plugin call) build only what
+// their query uses.
+enum : unsigned { kPartLt = 1u, kPartTcFp16 = 2u, kPartTcBf16 = 4u, kPartAll = 7u };
+
+static unsigned parts_for_query(const rg_query *q, int n)
+{
+    if (q->precision == RG_PREC_FP16X3) return kPartTcFp16;
+    if (q->precision == RG_PREC_BF16X3) return kPartTcBf16;
+    if (q->rng == RG_RNG_PHILOX && (n > fused_max_n() || env_contains("RG_PLAIN_KERNEL", "tiled"))) return kPartLt;
+    return 0u;
+}
+
+static int create_portfolio(int32_t n, const double *mu, const double *sigma, int64_t ld, const double *weights,
+                            int32_t flags, unsigned parts, rg_portfolio **out);
+
 int rg_portfolio_create(int32_t n, const double *mu, const double *sigma, int64_t ld,
                         const double *weights, int32_t flags, rg_portfolio **out)
+{
+    return create_portfolio(n, mu, sigma, ld, weights, flags, kPartAll, out);
+}
+
+static int create_portfolio(int32_t n, const double *mu, const double *sigma, int64_t ld, const double *weights,
+                            int32_t flags, unsigned parts, rg_portfolio **out)
 {
     if (!out) return set_error(RG_ERR_INVALID, "out is NULL");
     *out = nullptr;
@@ -361,9 +384,11 @@ int rg_portfolio_create(int32_t n, const double *mu, const double *sigma, int64_
     int st = get_ctx(&ctx, &dev);
     if (st) return st;
     const size_t nn = (size_t)n * n;
-    const size_t need = nn * 8 * (dev_in ? 1 : 2) + (size_t)n * 24 + (size_t)packed_len(n) * 4 +
-                        (size_t)tiled_kpad(n) * tiled_npad(n) * 4 +
-                        (n <= tc_max_n() ? 2 * tc_tile_bytes(n) : 0) + 64;
+    const bool want_lt = (parts & kPartLt) && n <= tiled_max_n();
+    const bool want_tc[2] = {(parts & kPartTcFp16) && n <= tc_max_n(), (parts & kPartTcBf16) && n <= tc_max_n()};
+    const size_t need = nn * 8 * (dev_in ? 1 : 2) + (size_t)n * 40 + (size_t)packed_len(n) * 4 +
+                        (want_lt ? (size_t)tiled_kpad(n) * tiled_npad(n) * 4 : 0) +
+                        (want_tc[0] ? tc_tile_bytes(n) : 0) + (want_tc[1] ? tc_tile_bytes(n) : 0) + 64;
     st = admit(need);
     if (st) return st;
 
@@ -381,13 +406,10 @@ int rg_portfolio_create(int32_t n, const double *mu, const double *sigma, int64_
     RG_CUDA_TRY(cudaMalloc(&p->d_L64, nn * sizeof(double)));
     RG_CUDA_TRY(cudaMalloc(&p->d_mu64, (size_t)n * sizeof(double)));
     RG_CUDA_TRY(cudaMalloc(&p->d_Lp, (size_t)packed_len(n) * sizeof(float)));
-    if (n <= tiled_max_n())
-        RG_CUDA_TRY(cudaMalloc(&p->d_Lt, (size_t)tiled_kpad(n) * tiled_npad(n) * sizeof(float)));
+    if (want_lt) RG_CUDA_TRY(cudaMalloc(&p->d_Lt, (size_t)tiled_kpad(n) * tiled_npad(n) * sizeof(float)));
     RG_CUDA_TRY(cudaMalloc(&p->d_err, sizeof(unsigned int)));
-    if (n <= tc_max_n()) {
-        RG_CUDA_TRY(cudaMalloc(&p->d_tc[0], tc_tile_bytes(n)));
-        RG_CUDA_TRY(cudaMalloc(&p->d_tc[1], tc_tile_bytes(n)));
-    }
+    if (want_tc[0]) RG_CUDA_TRY(cudaMalloc(&p->d_tc[0], tc_tile_bytes(n)));
+    if (want_tc[1]) RG_CUDA_TRY(cudaMalloc(&p->d_tc[1], tc_tile_bytes(n)));
     RG_CUDA_TRY(cudaMalloc(&p->d_w32, (size_t)n * sizeof(float)));
     RG_CUDA_TRY(cudaMalloc(&p->d_aux, (2 + 2 * (size_t)n) * sizeof(double))); // moments + factorisation scratch
     RG_CUDA_TRY(cudaMalloc(&p->d_info, sizeof(int)));
@@ -428,10 +450,8 @@ int rg_portfolio_create(int32_t n, const double *mu, const double *sigma, int64_
     p->wsw = aux[0];
     p->wmu = aux[1];
     if (p->d_Lt) RG_CUDA_TRY(launch_build_lt(p->d_L64, n, p->d_Lt, s));
-    if (p->d_tc[0]) {
-        RG_CUDA_TRY(launch_build_tc_tiles(p->d_L64, p->d_w32, n, 0, p->d_tc[0], s));
-        RG_CUDA_TRY(launch_build_tc_tiles(p->d_L64, p->d_w32, n, 1, p->d_tc[1], s));
-    }
+    if (p->d_tc[0]) RG_CUDA_TRY(launch_build_tc_tiles(p->d_L64, p->d_w32, n, 0, p->d_tc[0], s));
+    if (p->d_tc[1]) RG_CUDA_TRY(launch_build_tc_tiles(p->d_L64, p->d_w32, n, 1, p->d_tc[1], s));
     RG_CUDA_TRY(cudaMemsetAsync(p->d_err, 0, sizeof(unsigned int), s));
     RG_CUDA_TRY(cudaStreamSynchronize(s));
     p->h_Lp.resize((size_t)packed_len(n));
@@ -690,7 +710,7 @@ int rg_run(int32_t n, const double *mu, const double *sigma, int64_t ld, const d
     int st = validate_query(nullptr, q);
     if (st) return st;
     rg_portfolio *h = nullptr;
-    st = rg_portfolio_create(n, mu, sigma, ld, weights, 0, &h);
+    st = create_portfolio(n, mu, sigma, ld, weights, 0, parts_for_query(q, n), &h);
     if (st) return st;
     st = rg_simulate(h, q, out, nullptr);
     rg_portfolio_destroy(h);
@@ -734,7 +754,8 @@ int cuda_simulate(MonteCarloParams *params, MonteCarloResult *result)
     rg_portfolio *h = nullptr;
     rg_result r;
     int *d_s = nullptr;
-    int st = rg_portfolio_create(n, mu.data(), params->Sigma->data, (int64_t)params->Sigma->tda, nullptr, 0, &h);
+    int st = create_portfolio(n, mu.data(), params->Sigma->data, (int64_t)params->Sigma->tda, nullptr, 0,
+                              parts_for_query(&q, n), &h);
     if (st == RG_OK && want_s) {
         if (cudaMalloc(&d_s, (size_t)params->M * sizeof(int)) != cudaSuccess) {
             st = set_error(RG_ERR_NOMEM, "cudaMalloc of S_values failed");
