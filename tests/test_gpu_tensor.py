@@ -43,7 +43,8 @@ KERNELS = ["ws", "simple"]
 
 @pytest.mark.parametrize("kernel", KERNELS)
 @pytest.mark.parametrize("prec", ["fp16x3", "bf16x3"])
-@pytest.mark.parametrize("n,horizon,M", [(16, 1, 256), (64, 1, 1000), (130, 2, 777), (600, 10, 256)])
+@pytest.mark.parametrize("n,horizon,M", [(1, 1, 300), (16, 1, 256), (64, 1, 1000), (130, 2, 777), (600, 10, 256),
+                                         (640, 2, 200)])
 def test_tc_per_path_parity(gpu, oracle, monkeypatch, kernel, prec, n, horizon, M):
     monkeypatch.setenv("RG_TC_KERNEL", kernel)
     code, near_tol, port_tol = CASES[prec]
@@ -60,6 +61,23 @@ def test_tc_per_path_parity(gpu, oracle, monkeypatch, kernel, prec, n, horizon, 
     assert not bad.any(), f"{int(bad.sum())} paths differ; first {np.nonzero(bad)[0][:5]}"
     assert r["crash_count"] == int((S >= k).sum())
     assert r["breach_count"] == int((W < thr).sum())
+
+
+@pytest.mark.parametrize("kernel", KERNELS)
+def test_tc_path_ranges_add_up(gpu, monkeypatch, kernel):
+    """Counter-based draws: counts over [0, M) equal the sum over a split at
+    an offset that is not a multiple of the 64-path tile."""
+    monkeypatch.setenv("RG_TC_KERNEL", kernel)
+    mu, sigma, w = _case(300, 17)
+    port = gpu.Portfolio(mu, sigma, w)
+    M, cut = 50_000, 20_011
+    def run(n, off):
+        q = gpu.make_query(n, 41, x=0.03, k=20, horizon=3, port_threshold=-0.03, precision=3)
+        q.path_offset = off
+        return port.simulate(q)
+    whole, a, b = run(M, 0), run(cut, 0), run(M - cut, cut)
+    assert whole["crash_count"] == a["crash_count"] + b["crash_count"]
+    assert whole["breach_count"] == a["breach_count"] + b["breach_count"]
 
 
 @pytest.mark.parametrize("kernel", KERNELS)
@@ -148,6 +166,26 @@ def test_batch_equals_individual_queries(gpu, flags):
         assert (r2["crash_count"], r2["breach_count"]) == (r["crash_count"], r["breach_count"])
     inf = batch.info()
     assert inf["graph"] == (0 if flags else 1) and inf["items"] == 24
+
+
+def test_batch_mixed_precisions_and_draw_modes(gpu):
+    """One persistent launch over items that differ in precision (FP16x3 and
+    BF16x3), draw mode (daily, aggregated), horizon, asset count and path
+    budget: each item's counts equal the same query alone, in either order."""
+    from riskgpu import synth
+    ps = synth.batch_256(count=12, base_seed=99, n_max=600, m_range=(3e3, 3e4))
+    items = []
+    for i, p in enumerate(ps):
+        port = gpu.Portfolio(p.mu, p.sigma, p.weights)
+        q = gpu.make_query(p.n_paths, p.seed, x=p.x, k=p.k, horizon=p.horizon,
+                           port_threshold=p.port_threshold, precision=(3 if i % 2 == 0 else 1),
+                           draw_mode=(i // 2) % 2)
+        items.append((port, q))
+    alone = [port.simulate(q) for port, q in items]
+    for order in (list(range(12)), list(reversed(range(12)))):
+        res = gpu.Batch([items[i] for i in order]).run()
+        for i, r in zip(order, res):
+            assert (r["crash_count"], r["breach_count"]) == (alone[i]["crash_count"], alone[i]["breach_count"]), i
 
 
 def test_batch_autotuner_persists_choice(gpu, tmp_path, monkeypatch):
