@@ -165,8 +165,8 @@ static int capture(Batch *b)
 static int max_ctas_per_sm(const Batch *b)
 {
     int cols = 32;
-    while (cols < b->n_mt_max * 64) cols <<= 1;
-    const int by_tmem = 512 / cols, by_occ = tc_batch_occupancy(b->n_kt_max);
+    while (cols < b->n_mt_max * tc_batch_paths(b->n_mt_max)) cols <<= 1;
+    const int by_tmem = 512 / cols, by_occ = tc_batch_occupancy(b->n_mt_max);
     int c = by_occ < by_tmem ? by_occ : by_tmem;
     return c < 1 ? 1 : (c > 2 ? 2 : c);
 }
@@ -229,6 +229,14 @@ int rg_batch_create(const rg_batch_item *items, int32_t count, int32_t flags, rg
         return set_error(e == cudaErrorMemoryAllocation ? RG_ERR_NOMEM : RG_ERR_CUDA, "batch setup failed: %s",
                          cudaGetErrorString(e));
     }
+    // the tile width follows the largest item (tensor-memory columns)
+    for (int i = 0; i < count; i++) {
+        const Portfolio *p = reinterpret_cast<const Portfolio *>(items[i].portfolio);
+        const int kt = tc_k_tiles_of(p->n), mt = tc_row_tiles_of(p->n);
+        if (kt > b->n_kt_max) b->n_kt_max = kt;
+        if (mt > b->n_mt_max) b->n_mt_max = mt;
+    }
+    const int paths = tc_batch_paths(b->n_mt_max);
     long long tile = 0;
     for (int i = 0; i < count; i++) {
         const Portfolio *p = reinterpret_cast<const Portfolio *>(items[i].portfolio);
@@ -237,10 +245,7 @@ int rg_batch_create(const rg_batch_item *items, int32_t count, int32_t flags, rg
         PlainArgs a = query_args(p, &q, b->d_counts + 2 * (size_t)i);
         tc_fill_batch_item(host.data() + (size_t)i * tc_item_bytes(), a, p->d_tc[bf16], bf16,
                            q.draw_mode == RG_DRAWS_AGGREGATED, p->wmu, tile);
-        tile += tc_tiles_of(q.n_paths);
-        const int kt = tc_k_tiles_of(p->n), mt = tc_row_tiles_of(p->n);
-        if (kt > b->n_kt_max) b->n_kt_max = kt;
-        if (mt > b->n_mt_max) b->n_mt_max = mt;
+        tile += tc_tiles_of(q.n_paths, paths);
         b->queries.push_back(q);
     }
     b->total_tiles = tile;

@@ -192,7 +192,8 @@ size_t tc_tile_bytes(int n);
 void tc_fill_batch_item(void *item_out, const PlainArgs &a, const unsigned char *tiles, int bf16,
                         bool aggregated, double wmu, long long tile_begin);
 size_t tc_item_bytes();
-long long tc_tiles_of(long long n_paths);
+long long tc_tiles_of(long long n_paths, int paths_per_tile);
+int tc_batch_paths(int n_mt_max);
 int tc_row_tiles_of(int n);
 int tc_k_tiles_of(int n);
 cudaError_t launch_tc_batch(const void *d_items, int n_items, long long total_tiles, int unit_tiles,
@@ -200,7 +201,7 @@ cudaError_t launch_tc_batch(const void *d_items, int n_items, long long total_ti
                             cudaStream_t s, const long long *dyn = nullptr);
 int tc_max_k_tiles();
 cudaError_t tc_batch_prepare();
-int tc_batch_occupancy(int n_kt_max);
+int tc_batch_occupancy(int n_mt_max);
 // rg_mc_fused.cu: N <= 64 kernel, L in parameter space; Philox only.
 cudaError_t launch_fused(const PlainArgs &a, const float *Lp_host, const float *hmu, const float *w,
                          int sm_count, cudaStream_t s);

@@ -572,8 +572,20 @@ static constexpr int kWsProdWarp = 5;
 static constexpr int kWsGenWarp0 = 6;
 static constexpr int kWsGenThreads = kWsThreads - 32 * kWsGenWarp0;
 static constexpr int kTcMaxMt = (kTcMaxKt * kTcKt + 1 + kTcRows - 1) / kTcRows;
-static constexpr int kWsZSlots = 4;  // K-tile slots of Z (hi + lo, 16 KB each)
-static constexpr int kWsStages = 5;  // Lhat ring stages (hi + lo, 32 KB each)
+static constexpr int kWsZSlots = 4; // K-tile slots of Z (hi + lo, P x 64 x 2 bytes each part)
+
+// Paths per tile P (the MMA's N): 96 when the item's row tiles fit in tensor
+// memory at that width (n_mt x 96 <= 512 columns, N <= 639), else 64.  A
+// 96-path tile moves 7 KB of operands per 1.5x the work of a 64-path MMA
+// (6 KB) and streams each Lhat tile once per 96 paths; its Z ring (96 KB)
+// leaves room for 4 Lhat stages, the 64-path form's (64 KB) for 5.
+template <int P> struct WsShape {
+    static constexpr int kZBytes = P * kTcKt * 2;          // one part of a Z K tile
+    static constexpr int kStages = (P == 64) ? 5 : 4;      // Lhat ring stages (hi + lo, 32 KB each)
+    static constexpr size_t kSmem = 1024 + (size_t)kWsZSlots * 2 * kZBytes + (size_t)kStages * 2 * kTcTileBytes;
+    static_assert(P % 16 == 0 && P >= 64 && P <= 128, "path tile");
+    static_assert(kSmem <= 227 * 1024 - 2048, "shared memory");
+};
 
 __device__ __forceinline__ void named_sync(int id, int n)
 {
@@ -599,23 +611,25 @@ __device__ __forceinline__ int tc_kts(int mt, int n_mt, int n_kt)
     return (mt == n_mt - 1) ? n_kt : min(n_kt, (kTcRows * (mt + 1) + kTcKt - 1) / kTcKt);
 }
 
-template <bool VAR, bool BATCH>
+template <bool VAR, bool BATCH, int P>
 __global__ void __launch_bounds__(kWsThreads, 1) mc_tcws_kernel(const __grid_constant__ TcBatch b)
 {
+    using Sh = WsShape<P>;
+    constexpr int kStages = Sh::kStages, kZB = Sh::kZBytes;
     extern __shared__ __align__(1024) unsigned char tc_smem[];
     const PlainArgs &a = b.var;
     unsigned char *base = (unsigned char *)(((uintptr_t)tc_smem + 1023) & ~(uintptr_t)1023);
     unsigned char *zhi = base;
-    unsigned char *zlo = zhi + kWsZSlots * kTcZBytes;
-    unsigned char *lst = zlo + kWsZSlots * kTcZBytes;
+    unsigned char *zlo = zhi + kWsZSlots * kZB;
+    unsigned char *lst = zlo + kWsZSlots * kZB;
 
-    __shared__ __align__(8) uint64_t full_bar[kWsStages], empty_bar[kWsStages];
+    __shared__ __align__(8) uint64_t full_bar[kStages], empty_bar[kStages];
     __shared__ __align__(8) uint64_t zfull[kWsZSlots], zempty[kWsZSlots];
     __shared__ __align__(8) uint64_t acc_full[kTcMaxMt], acc_free[kTcMaxMt];
     __shared__ __align__(8) uint64_t tile_pub[2], slot_free[2], drain_bar;
     __shared__ uint32_t tmem_base_sh;
-    __shared__ int sS[kTcPaths];
-    __shared__ float sPort[kTcPaths];
+    __shared__ int sS[P];
+    __shared__ float sPort[P];
     // set by a role whose bounded wait ran out; the others then make no
     // further waits and finish
     __shared__ int tm_abort;
@@ -627,12 +641,12 @@ __global__ void __launch_bounds__(kWsThreads, 1) mc_tcws_kernel(const __grid_con
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
     const int ncols = b.tmem_cols;
     if (tid < 4) sacc[tid] = 0ull;
-    if (tid < kTcPaths) {
+    if (tid < P) {
         sS[tid] = 0;
         sPort[tid] = 0.f;
     }
     if (tid == 0) {
-        for (int s = 0; s < kWsStages; s++) {
+        for (int s = 0; s < kStages; s++) {
             mbar_init(&full_bar[s], 1);
             mbar_init(&empty_bar[s], 1);
         }
@@ -725,7 +739,7 @@ __global__ void __launch_bounds__(kWsThreads, 1) mc_tcws_kernel(const __grid_con
             if (tile < 0) break; // uniform: every thread read the same s_tile
             const TcItem &it = BATCH ? s_item[slot] : b.one;
             const int n = it.n, nq = (n + 3) >> 2, n_kt = it.n_kt;
-            const long long p0 = (tile - it.tile_begin) * kTcPaths;
+            const long long p0 = (tile - it.tile_begin) * P;
             // each thread walks its items of the tile in K-tile order and
             // arrives on zfull[kt] once it has written its share of kt (no
             // group barrier, so no thread idles at K-tile boundaries)
@@ -737,13 +751,13 @@ __global__ void __launch_bounds__(kWsThreads, 1) mc_tcws_kernel(const __grid_con
                     atomicOr(b.err, 16u);
                     gab = 1;
                 }
-                const int per_kt = kTcPaths * (kTcKt / 4);
+                const int per_kt = P * (kTcKt / 4);
                 // items of this thread in kt: global item index i = kt*per_kt + local,
                 // assigned round robin over the whole tile (i % kWsGenThreads == gtid)
                 int first = gtid - (kt * per_kt) % kWsGenThreads;
                 if (first < 0) first += kWsGenThreads;
                 for (int item = first; item < per_kt; item += kWsGenThreads) {
-                    const int p = item & (kTcPaths - 1), q = kt * (kTcKt / 4) + (item >> 6);
+                    const int ql = item / P, p = item - ql * P, q = kt * (kTcKt / 4) + ql;
                     const unsigned long long path = it.path0 + (unsigned long long)(p0 + p);
                     const uint32_t plo = (uint32_t)path, phi = (uint32_t)(path >> 32);
                     float z[4] = {0.f, 0.f, 0.f, 0.f};
@@ -764,7 +778,7 @@ __global__ void __launch_bounds__(kWsThreads, 1) mc_tcws_kernel(const __grid_con
                     }
                     unsigned short h[4], l[4];
                     for (int e = 0; e < 4; e++) split2(z[e], it.bf16, h[e], l[e]);
-                    const uint32_t off = (uint32_t)zs * kTcZBytes + sw128_offset(p, 4 * (item >> 6));
+                    const uint32_t off = (uint32_t)zs * kZB + sw128_offset(p, 4 * ql);
                     *reinterpret_cast<uint2 *>(zhi + off) =
                         make_uint2((uint32_t)h[0] | ((uint32_t)h[1] << 16), (uint32_t)h[2] | ((uint32_t)h[3] << 16));
                     *reinterpret_cast<uint2 *>(zlo + off) =
@@ -793,8 +807,8 @@ __global__ void __launch_bounds__(kWsThreads, 1) mc_tcws_kernel(const __grid_con
                 for (int kt = 0; kt < n_kt && !tm_abort; kt++) {
                     for (int mt = 0; mt < n_mt; mt++) {
                         if (kt >= tc_kts(mt, n_mt, n_kt)) continue;
-                        const int s = prod_iter % kWsStages;
-                        if (tm_abort || !mbar_wait(&empty_bar[s], ((prod_iter / kWsStages) & 1u) ^ 1u)) {
+                        const int s = prod_iter % kStages;
+                        if (tm_abort || !mbar_wait(&empty_bar[s], ((prod_iter / kStages) & 1u) ^ 1u)) {
                             atomicOr(b.err, 1u);
                             tm_abort = 1;
                             break;
@@ -813,8 +827,8 @@ __global__ void __launch_bounds__(kWsThreads, 1) mc_tcws_kernel(const __grid_con
                 }
             }
             // the copies still in flight land before the kernel ends
-            for (unsigned i = prod_iter > kWsStages ? prod_iter - kWsStages : 0; i < prod_iter; i++)
-                if ((int)i != skipped) mbar_wait(&full_bar[i % kWsStages], (i / kWsStages) & 1u);
+            for (unsigned i = prod_iter > kStages ? prod_iter - kStages : 0; i < prod_iter; i++)
+                if ((int)i != skipped) mbar_wait(&full_bar[i % kStages], (i / kStages) & 1u);
         }
         __syncwarp();
     } else if (warp == kWsMmaWarp) {
@@ -833,7 +847,7 @@ __global__ void __launch_bounds__(kWsThreads, 1) mc_tcws_kernel(const __grid_con
                 if (s_tile[slot] < 0) break;
                 const TcItem &it = BATCH ? s_item[slot] : b.one;
                 const int n_kt = it.n_kt, n_mt = it.n_mt;
-                const uint32_t idesc = tc_idesc(it.bf16, kTcRows, kTcPaths);
+                const uint32_t idesc = tc_idesc(it.bf16, kTcRows, P);
                 for (int kt = 0; kt < n_kt && !tm_abort; kt++) {
                     const unsigned g = g0 + (unsigned)kt;
                     const int zs = (int)(g % kWsZSlots);
@@ -843,8 +857,8 @@ __global__ void __launch_bounds__(kWsThreads, 1) mc_tcws_kernel(const __grid_con
                         break;
                     }
                     tc_fence_after();
-                    const uint32_t zh_lo = sw128_desc_lo(smem_u32(zhi + (size_t)zs * kTcZBytes));
-                    const uint32_t zl_lo = sw128_desc_lo(smem_u32(zlo + (size_t)zs * kTcZBytes));
+                    const uint32_t zh_lo = sw128_desc_lo(smem_u32(zhi + (size_t)zs * kZB));
+                    const uint32_t zl_lo = sw128_desc_lo(smem_u32(zlo + (size_t)zs * kZB));
                     for (int mt = 0; mt < n_mt; mt++) {
                         const int kts = tc_kts(mt, n_mt, n_kt);
                         if (kt >= kts) continue;
@@ -860,10 +874,10 @@ __global__ void __launch_bounds__(kWsThreads, 1) mc_tcws_kernel(const __grid_con
                             break;
                         }
                         tc_fence_after();
-                        tc_mma_pair(tmem + (uint32_t)(mt * kTcPaths), lst_lo + (uint32_t)rs * (2 * kTcTileBytes >> 4),
+                        tc_mma_pair(tmem + (uint32_t)(mt * P), lst_lo + (uint32_t)rs * (2 * kTcTileBytes >> 4),
                                     zh_lo, zl_lo, idesc, kt > 0 ? 1u : 0u);
                         tc_commit(&empty_bar[rs]);
-                        if (++rs == kWsStages) {
+                        if (++rs == kStages) {
                             rs = 0;
                             rph ^= 1u;
                         }
@@ -914,8 +928,8 @@ __global__ void __launch_bounds__(kWsThreads, 1) mc_tcws_kernel(const __grid_con
                 const bool asset = row < n;
                 const float thr = asset ? tc_threshold(it, row) : 0.f;
 #pragma unroll
-                for (int cb = 0; cb < kTcPaths / 16; cb++) {
-                    const uint32_t taddr = tmem + ((uint32_t)(warp * 32) << 16) + (uint32_t)(mt * kTcPaths + cb * 16);
+                for (int cb = 0; cb < P / 16; cb++) {
+                    const uint32_t taddr = tmem + ((uint32_t)(warp * 32) << 16) + (uint32_t)(mt * P + cb * 16);
                     uint32_t v[16];
                     asm volatile("tcgen05.ld.sync.aligned.32x32b.x16.b32 "
                                  "{%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, [%16];"
@@ -948,8 +962,8 @@ __global__ void __launch_bounds__(kWsThreads, 1) mc_tcws_kernel(const __grid_con
             }
             apar ^= (1u << n_mt) - 1u;
             named_sync(1, 32 * kWsEpiWarps); // every count of the tile is in sS / sPort
-            if (tid < kTcPaths) {
-                const long long p = (tile - it.tile_begin) * kTcPaths + tid;
+            if (tid < P) {
+                const long long p = (tile - it.tile_begin) * P + tid;
                 int crash = 0, breach = 0;
                 if (p < it.n_paths) {
                     const int S = sS[tid];
@@ -1031,22 +1045,21 @@ cudaError_t launch_build_tc_tiles(const double *L64, const float *w32, int n, in
     return cudaGetLastError();
 }
 
-static int tmem_cols_for(int n_mt)
+static int tmem_cols_for(int n_mt, int paths)
 {
     int c = 32;
-    while (c < n_mt * kTcPaths) c <<= 1;
+    while (c < n_mt * paths) c <<= 1;
     return c;
-}
-
-static size_t ws_smem_bytes()
-{
-    return 1024 + (size_t)kWsZSlots * 2 * kTcZBytes + (size_t)kWsStages * 2 * kTcTileBytes;
 }
 
 static size_t tc_smem_bytes(int n_kt_max)
 {
     return 1024 + (size_t)n_kt_max * 2 * kTcZBytes + (size_t)kTcStages * 2 * kTcTileBytes;
 }
+
+// Paths per tile of the warp-specialised kernel for items of at most
+// n_mt_max row tiles (tensor memory holds n_mt x paths FP32 columns).
+int tc_batch_paths(int n_mt_max) { return n_mt_max * 96 <= 512 ? 96 : 64; }
 
 static void fill_item(TcItem &it, const PlainArgs &a, const unsigned char *tiles, int bf16, bool aggregated,
                       double wmu, long long tile_begin)
@@ -1076,6 +1089,15 @@ static void fill_item(TcItem &it, const PlainArgs &a, const unsigned char *tiles
     it.sqrt_h = sqrtf((float)a.horizon);
 }
 
+template <class K>
+static cudaError_t launch_one(K kern, const TcBatch &b, int threads, size_t smem, long long grid, cudaStream_t s)
+{
+    cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e != cudaSuccess) return e;
+    kern<<<(unsigned)grid, threads, smem, s>>>(b);
+    return cudaGetLastError();
+}
+
 cudaError_t launch_tc(const PlainArgs &a, const unsigned char *tiles, int bf16, bool aggregated, double wmu,
                       unsigned int *err, bool inject_stall, int sm_count, cudaStream_t s)
 {
@@ -1086,31 +1108,34 @@ cudaError_t launch_tc(const PlainArgs &a, const unsigned char *tiles, int bf16, 
     b.items = nullptr;
     b.n_items = 1;
     b.unit_tiles = 1;
-    b.total_tiles = (a.n_paths + kTcPaths - 1) / kTcPaths;
     b.work = nullptr;
     b.err = err;
     b.inject_stall = inject_stall ? 1 : 0;
     b.n_kt_max = b.one.n_kt;
-    b.tmem_cols = tmem_cols_for(b.one.n_mt);
     b.var = a;
-    if (b.one.n_mt * kTcPaths > 512) return cudaErrorInvalidValue;
-    // The warp-specialised kernel: generation, MMAs and the per-row-tile
-    // epilogue overlap.  RG_TC_KERNEL=simple selects the phase-serial kernel
-    // (generate, multiply, read back in turn), kept as a second
-    // implementation that the tests compare.
+    // The warp-specialised kernel (96-path tiles where tensor memory allows,
+    // else 64): generation, MMAs and the per-row-tile epilogue overlap.
+    // RG_TC_KERNEL=simple selects the phase-serial kernel (64-path tiles:
+    // generate, multiply, read back in turn), kept as a second
+    // implementation that the tests compare; RG_TC_KERNEL=ws64 forces the
+    // warp-specialised kernel's 64-path form.
     const char *sel = getenv("RG_TC_KERNEL");
-    bool simple = false;
-    if (sel && strstr(sel, "simple")) simple = true;
-    if (sel && strstr(sel, "ws")) simple = false;
-    auto kern = simple ? ((a.var_mode != 0) ? mc_tc_kernel<true, false> : mc_tc_kernel<false, false>)
-                       : ((a.var_mode != 0) ? mc_tcws_kernel<true, false> : mc_tcws_kernel<false, false>);
-    const size_t smem = simple ? tc_smem_bytes(b.n_kt_max) : ws_smem_bytes();
-    cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-    if (e != cudaSuccess) return e;
+    const bool simple = sel && strstr(sel, "simple");
+    const int paths = simple || (sel && strstr(sel, "ws64")) ? 64 : tc_batch_paths(b.one.n_mt);
+    b.total_tiles = (a.n_paths + paths - 1) / paths;
+    b.tmem_cols = tmem_cols_for(b.one.n_mt, paths);
+    if (b.one.n_mt * paths > 512) return cudaErrorInvalidValue;
     long long grid = sm_count;
     if (b.total_tiles < grid) grid = b.total_tiles;
-    kern<<<(unsigned)grid, simple ? kTcThreads : kWsThreads, smem, s>>>(b);
-    return cudaGetLastError();
+    const bool var = a.var_mode != 0;
+    if (simple)
+        return var ? launch_one(mc_tc_kernel<true, false>, b, kTcThreads, tc_smem_bytes(b.n_kt_max), grid, s)
+                   : launch_one(mc_tc_kernel<false, false>, b, kTcThreads, tc_smem_bytes(b.n_kt_max), grid, s);
+    if (paths == 96)
+        return var ? launch_one(mc_tcws_kernel<true, false, 96>, b, kWsThreads, WsShape<96>::kSmem, grid, s)
+                   : launch_one(mc_tcws_kernel<false, false, 96>, b, kWsThreads, WsShape<96>::kSmem, grid, s);
+    return var ? launch_one(mc_tcws_kernel<true, false, 64>, b, kWsThreads, WsShape<64>::kSmem, grid, s)
+               : launch_one(mc_tcws_kernel<false, false, 64>, b, kWsThreads, WsShape<64>::kSmem, grid, s);
 }
 
 // Host-side description of one batch item for tc_batch_items.
@@ -1120,13 +1145,15 @@ void tc_fill_batch_item(void *item_out, const PlainArgs &a, const unsigned char 
     fill_item(*reinterpret_cast<TcItem *>(item_out), a, tiles, bf16, aggregated, wmu, tile_begin);
 }
 size_t tc_item_bytes() { return sizeof(TcItem); }
-long long tc_tiles_of(long long n_paths) { return (n_paths + kTcPaths - 1) / kTcPaths; }
+long long tc_tiles_of(long long n_paths, int paths) { return (n_paths + paths - 1) / paths; }
 int tc_row_tiles_of(int n) { return tc_row_tiles(n); }
 int tc_k_tiles_of(int n) { return tc_k_tiles(n); }
 
 // One persistent launch over many items: CTAs claim units of `unit_tiles`
-// tiles from *work (zeroed by the caller).  tc_batch_prepare() must have
-// run (it is not a stream operation, so it stays out of graph captures).
+// tiles from *work (zeroed by the caller).  The items' tiles must have been
+// numbered with tc_batch_paths(n_mt_max) paths per tile.  tc_batch_prepare()
+// must have run (it is not a stream operation, so it stays out of graph
+// captures).
 cudaError_t launch_tc_batch(const void *d_items, int n_items, long long total_tiles, int unit_tiles,
                             unsigned int *work, unsigned int *err, int n_kt_max, int n_mt_max, int grid,
                             cudaStream_t s, const long long *dyn)
@@ -1141,31 +1168,42 @@ cudaError_t launch_tc_batch(const void *d_items, int n_items, long long total_ti
     b.work = work;
     b.err = err;
     b.n_kt_max = n_kt_max;
-    b.tmem_cols = tmem_cols_for(n_mt_max);
-    if (n_mt_max * kTcPaths > 512 || n_kt_max > kTcMaxKt) return cudaErrorInvalidValue;
-    mc_tcws_kernel<false, true><<<(unsigned)grid, kWsThreads, ws_smem_bytes(), s>>>(b);
+    const int paths = tc_batch_paths(n_mt_max);
+    b.tmem_cols = tmem_cols_for(n_mt_max, paths);
+    if (n_mt_max * paths > 512 || n_kt_max > kTcMaxKt) return cudaErrorInvalidValue;
+    if (paths == 96)
+        mc_tcws_kernel<false, true, 96><<<(unsigned)grid, kWsThreads, WsShape<96>::kSmem, s>>>(b);
+    else
+        mc_tcws_kernel<false, true, 64><<<(unsigned)grid, kWsThreads, WsShape<64>::kSmem, s>>>(b);
     return cudaGetLastError();
 }
 
-// Resident CTAs per SM of the batched kernel (registers and shared memory,
-// which the warp-specialised kernel sizes independently of the items;
-// tensor memory is checked by the caller).
-int tc_batch_occupancy(int n_kt_max)
+// Resident CTAs per SM of the batched kernel for items of at most n_mt_max
+// row tiles (registers and shared memory; tensor memory is checked by the
+// caller).
+int tc_batch_occupancy(int n_mt_max)
 {
-    (void)n_kt_max;
     int per_sm = 0;
-    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, mc_tcws_kernel<false, true>, kWsThreads,
-                                                      ws_smem_bytes()) != cudaSuccess)
-        return 1;
+    const cudaError_t e =
+        tc_batch_paths(n_mt_max) == 96
+            ? cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, mc_tcws_kernel<false, true, 96>, kWsThreads,
+                                                            WsShape<96>::kSmem)
+            : cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, mc_tcws_kernel<false, true, 64>, kWsThreads,
+                                                            WsShape<64>::kSmem);
+    if (e != cudaSuccess) return 1;
     return per_sm < 1 ? 1 : per_sm;
 }
 
-// Raise the kernel's dynamic shared-memory limit to the largest size a
-// batch can ask for; called once before any launch or capture.
+// Raise the batched kernels' dynamic shared-memory limit; called once
+// before any launch or capture.
 cudaError_t tc_batch_prepare()
 {
-    return cudaFuncSetAttribute(mc_tcws_kernel<false, true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                (int)ws_smem_bytes());
+    cudaError_t e = cudaFuncSetAttribute(mc_tcws_kernel<false, true, 96>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                         (int)WsShape<96>::kSmem);
+    if (e == cudaSuccess)
+        e = cudaFuncSetAttribute(mc_tcws_kernel<false, true, 64>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                 (int)WsShape<64>::kSmem);
+    return e;
 }
 
 } // namespace rg

@@ -89,6 +89,10 @@ struct Server {
     int fatal = RG_OK;
 };
 
+// Row tiles of the largest servable portfolio: five (N <= 639) keeps the
+// slots' launches at 96-path tiles (tensor memory: 5 x 96 columns).
+static constexpr int kServedMaxRowTiles = 5;
+
 static int slot_init(Server *sv, Slot &sl)
 {
     const int cap = sv->cfg.max_batch_items;
@@ -113,7 +117,7 @@ static int slot_init(Server *sv, Slot &sl)
         if (e2 == cudaSuccess) e2 = cudaMemsetAsync(sl.d_work, 0, 2 * sizeof(unsigned int), sl.stream);
         if (e2 == cudaSuccess)
             e2 = launch_tc_batch(sl.d_items, cap, 0, 1, sl.d_work, sl.d_work + 1, tc_max_k_tiles(),
-                                 tc_row_tiles_of(tc_max_n()), sv->sm_count, sl.stream, sl.d_dyn);
+                                 kServedMaxRowTiles, sv->sm_count, sl.stream, sl.d_dyn);
         if (e2 == cudaSuccess)
             e2 = cudaMemcpyAsync(sl.h_counts, sl.d_counts, 16 * (size_t)cap, cudaMemcpyDeviceToHost, sl.stream);
         if (e2 == cudaSuccess)
@@ -233,7 +237,7 @@ static bool schedule_once(Server *sv)
             PlainArgs a = query_args(p, &rq.q, sl.d_counts + 2 * (size_t)n);
             tc_fill_batch_item(sl.h_items + (size_t)n * tc_item_bytes(), a, p->d_tc[bf16], bf16,
                                rq.q.draw_mode == RG_DRAWS_AGGREGATED, p->wmu, tile);
-            tile += tc_tiles_of(rq.q.n_paths);
+            tile += tc_tiles_of(rq.q.n_paths, tc_batch_paths(kServedMaxRowTiles));
             sl.tickets.push_back(tk);
             n++;
         }
@@ -332,8 +336,9 @@ int rg_server_register(rg_server *h, int32_t portfolio_id, const rg_portfolio *p
     if (!h || !p) return set_error(RG_ERR_INVALID, "NULL argument");
     Server *sv = reinterpret_cast<Server *>(h);
     const Portfolio *pp = reinterpret_cast<const Portfolio *>(p);
-    if (pp->n > tc_max_n() || !pp->d_tc[0])
-        return set_error(RG_ERR_UNSUPPORTED, "served portfolios are limited to N <= %d", tc_max_n());
+    const int max_n = kServedMaxRowTiles * 128 - 1; // row N (w^T L) shares the last row tile
+    if (pp->n > max_n || tc_row_tiles_of(pp->n) > kServedMaxRowTiles || !pp->d_tc[0] || !pp->d_tc[1])
+        return set_error(RG_ERR_UNSUPPORTED, "served portfolios are limited to N <= %d", max_n);
     std::lock_guard<std::mutex> lk(sv->mu);
     sv->portfolios[portfolio_id] = pp;
     return RG_OK;

@@ -201,7 +201,7 @@ int rg_batch_destroy(rg_batch *b);
  * max_batch_items requests each) and launched while earlier batches may
  * still be running; completions are polled every poll_us.  A request's
  * result does not depend on the batch that carried it (draws are keyed by
- * seed and path index).  Requests use the Philox layout, N <= 640, no VaR;
+ * seed and path index).  Requests use the Philox layout, N <= 639, no VaR;
  * the portfolios stay owned by the caller and must outlive the server. */
 typedef struct rg_server rg_server;
 typedef struct {

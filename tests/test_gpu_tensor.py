@@ -36,9 +36,10 @@ def _case(n, seed):
     return mu, sigma, w
 
 
-# the two tcgen05 kernels: "ws" (warp-specialised, the default) and "simple"
-# (phase-serial); RG_TC_KERNEL forces one of them
-KERNELS = ["ws", "simple"]
+# the tcgen05 kernels: "ws" (warp-specialised, the default: 96-path tiles up
+# to five row tiles, N <= 639), "ws64" (its 64-path form) and "simple"
+# (phase-serial, 64-path tiles); RG_TC_KERNEL forces one of them
+KERNELS = ["ws", "ws64", "simple"]
 
 
 @pytest.mark.parametrize("kernel", KERNELS)
