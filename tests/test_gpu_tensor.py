@@ -189,6 +189,39 @@ def test_batch_mixed_precisions_and_draw_modes(gpu):
             assert (r["crash_count"], r["breach_count"]) == (alone[i]["crash_count"], alone[i]["breach_count"]), i
 
 
+def test_batch_with_six_row_tiles_uses_64_path_tiles(gpu):
+    """An N = 640 item (six row tiles: 6 x 96 columns would not fit in
+    tensor memory) moves the whole batch to 64-path tiles; counts still
+    equal the queries alone."""
+    items = []
+    for i, n in enumerate((640, 37, 300)):
+        mu, sigma, w = _case(n, 50 + i)
+        port = gpu.Portfolio(mu, sigma, w)
+        q = gpu.make_query(9_000 + 1_000 * i, 7 + i, x=0.03, k=max(1, n // 12), horizon=2,
+                           port_threshold=-0.03, precision=3)
+        items.append((port, q))
+    res = gpu.Batch(items).run()
+    for (port, q), r in zip(items, res):
+        alone = port.simulate(q)
+        assert (r["crash_count"], r["breach_count"]) == (alone["crash_count"], alone["breach_count"])
+
+
+def test_server_rejects_six_row_tiles(gpu):
+    """The served form runs 96-path tiles: N = 640 is refused at
+    registration, N = 639 is accepted."""
+    srv = gpu.Server()
+    try:
+        mu, sigma, w = _case(640, 3)
+        with pytest.raises(gpu.RiskGpuError) as e:
+            srv.register(1, gpu.Portfolio(mu, sigma, w))
+        assert e.value.status == gpu.RG_ERR_UNSUPPORTED
+        mu, sigma, w = _case(639, 3)
+        port = gpu.Portfolio(mu, sigma, w)
+        srv.register(2, port)
+    finally:
+        srv.close()
+
+
 def test_batch_autotuner_persists_choice(gpu, tmp_path, monkeypatch):
     monkeypatch.setenv("RG_TUNE_CACHE", str(tmp_path / "tune.json"))
     ps, items = _batch_items(gpu, 12, seed=7)
