@@ -312,6 +312,9 @@ def engine_arm(args):
     e2e_steps = max(3, min(args.steps, 5))
     os.environ.pop("RG_MATERIALIZE_S", None)
     os.environ.pop("RG_RNG", None)
+    # every step uploads and factors its inputs: the plugin path's cache of
+    # resident factors is off for this measurement
+    os.environ["RG_PLUGIN_CACHE"] = "0"
     if args.workload == "one_factor_50":
         call = riskgpu.PluginCall(p.mu, p.sigma)
         run_once = lambda: call.run(args.paths, p.k, p.x, p.seed)["status"]

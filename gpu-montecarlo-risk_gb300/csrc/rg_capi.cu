@@ -18,6 +18,7 @@
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
+#include <memory>
 #include <mutex>
 #include <vector>
 
@@ -718,6 +719,88 @@ int rg_run(int32_t n, const double *mu, const double *sigma, int64_t ld, const d
 }
 
 // ------------------------------------------------------------- drop-in
+// Resident factors of the plugin path.  main_runner hands the same mu and
+// Sigma to every model it runs, and each call of run_model would otherwise
+// upload and factor them again.  A few recent (mu, Sigma, parts) are kept
+// with their device portfolio; a hit compares the inputs in full (no hash
+// is trusted), so a changed input always refactors.  Entries are shared
+// pointers: an evicted factor is freed when its last call finishes.
+// RG_PLUGIN_CACHE=0 turns the cache off.  Entries live until the process
+// exits.
+namespace {
+using PortfolioRef = std::shared_ptr<rg_portfolio>;
+struct PluginEntry {
+    int n = 0;
+    int dev = -1;
+    unsigned parts = 0;
+    std::vector<double> mu, sigma; // sigma packed n x n
+    PortfolioRef port;
+    unsigned long long last_use = 0;
+};
+std::mutex g_plugin_mu;
+// never destroyed: no CUDA call runs during static destruction at exit
+std::vector<PluginEntry> &g_plugin_cache = *new std::vector<PluginEntry>();
+unsigned long long g_plugin_clock = 0;
+constexpr size_t kPluginCacheEntries = 4;
+
+bool same_inputs(const PluginEntry &e, int n, int dev, unsigned parts, const double *mu, const double *sigma,
+                 long long tda)
+{
+    if (e.n != n || e.dev != dev || e.parts != parts) return false;
+    if (memcmp(e.mu.data(), mu, sizeof(double) * (size_t)n) != 0) return false;
+    for (int i = 0; i < n; i++)
+        if (memcmp(e.sigma.data() + (size_t)i * n, sigma + (size_t)i * tda, sizeof(double) * (size_t)n) != 0)
+            return false;
+    return true;
+}
+} // namespace
+
+// The portfolio for a plugin call: from the cache, or created (and cached
+// unless RG_PLUGIN_CACHE=0).
+static int plugin_portfolio(int n, const double *mu, const double *sigma, long long tda, unsigned parts,
+                            PortfolioRef *out)
+{
+    const char *env = getenv("RG_PLUGIN_CACHE");
+    const bool use_cache = !(env && env[0] == '0');
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess) {
+        cudaGetLastError();
+        dev = -1;
+    }
+    if (use_cache) {
+        std::lock_guard<std::mutex> lk(g_plugin_mu);
+        for (PluginEntry &e : g_plugin_cache)
+            if (same_inputs(e, n, dev, parts, mu, sigma, tda)) {
+                e.last_use = ++g_plugin_clock;
+                *out = e.port;
+                return RG_OK;
+            }
+    }
+    rg_portfolio *h = nullptr;
+    const int st = create_portfolio(n, mu, sigma, tda, nullptr, 0, parts, &h);
+    if (st != RG_OK) return st;
+    PortfolioRef ref(h, [](rg_portfolio *x) { rg_portfolio_destroy(x); });
+    *out = ref;
+    if (!use_cache) return RG_OK;
+    std::lock_guard<std::mutex> lk(g_plugin_mu);
+    if (g_plugin_cache.size() >= kPluginCacheEntries)
+        g_plugin_cache.erase(std::min_element(
+            g_plugin_cache.begin(), g_plugin_cache.end(),
+            [](const PluginEntry &x, const PluginEntry &y) { return x.last_use < y.last_use; }));
+    PluginEntry e;
+    e.n = n;
+    e.dev = dev;
+    e.parts = parts;
+    e.mu.assign(mu, mu + n);
+    e.sigma.resize((size_t)n * n);
+    for (int i = 0; i < n; i++)
+        memcpy(e.sigma.data() + (size_t)i * n, sigma + (size_t)i * tda, sizeof(double) * (size_t)n);
+    e.port = ref;
+    e.last_use = ++g_plugin_clock;
+    g_plugin_cache.push_back(std::move(e));
+    return RG_OK;
+}
+
 int cuda_simulate(MonteCarloParams *params, MonteCarloResult *result)
 {
     if (!params || !result) {
@@ -754,8 +837,10 @@ int cuda_simulate(MonteCarloParams *params, MonteCarloResult *result)
     rg_portfolio *h = nullptr;
     rg_result r;
     int *d_s = nullptr;
-    int st = create_portfolio(n, mu.data(), params->Sigma->data, (int64_t)params->Sigma->tda, nullptr, 0,
-                              parts_for_query(&q, n), &h);
+    PortfolioRef ref;
+    int st = plugin_portfolio(n, mu.data(), params->Sigma->data, (long long)params->Sigma->tda,
+                              parts_for_query(&q, n), &ref);
+    h = ref.get();
     if (st == RG_OK && want_s) {
         if (cudaMalloc(&d_s, (size_t)params->M * sizeof(int)) != cudaSuccess) {
             st = set_error(RG_ERR_NOMEM, "cudaMalloc of S_values failed");
@@ -770,7 +855,7 @@ int cuda_simulate(MonteCarloParams *params, MonteCarloResult *result)
             st = set_error(RG_ERR_NOMEM, "copy of S_values failed");
     }
     if (d_s) cudaFree(d_s);
-    rg_portfolio_destroy(h);
+    ref.reset();
     if (st != RG_OK) {
         fprintf(stderr, "Error: CUDA model failed: %s (%s)\n", rg_status_string(st), rg_last_error());
         return -1;

@@ -246,6 +246,36 @@ def test_plugin_drop_in(gpu, oracle, monkeypatch):
     assert r["count"] == int((r["S"] >= p.k).sum())
 
 
+def test_plugin_cache_of_resident_factors(gpu, monkeypatch):
+    """run_model keeps recent factors resident: a repeated call gives the
+    same counts as a call that uploads and factors anew (RG_PLUGIN_CACHE=0);
+    a Sigma changed in place is refactored, not served from the cache; more
+    distinct inputs than cache entries still give the right counts."""
+    from riskgpu import synth
+    p = synth.one_factor_50(n_paths=1)
+    call = gpu.PluginCall(p.mu, p.sigma)
+    args = (200_000, p.k, p.x, p.seed)
+
+    def fresh(c):
+        monkeypatch.setenv("RG_PLUGIN_CACHE", "0")
+        r = c.run(*args)
+        monkeypatch.delenv("RG_PLUGIN_CACHE")
+        return r
+
+    ref = fresh(call)
+    a, b = call.run(*args), call.run(*args)
+    assert a["count"] == b["count"] == ref["count"]
+    call.sigma[:, :] = call.sigma * 1.8      # same buffer, new values: more crashes
+    c = call.run(*args)
+    assert c["count"] == fresh(call)["count"] and c["count"] > a["count"]
+    rng = np.random.default_rng(8)
+    for i in range(6):
+        mu, sigma, _, _ = synth.one_factor_sigma(rng, 20 + i)
+        ci = gpu.PluginCall(mu, sigma)
+        assert ci.run(*args)["count"] == fresh(ci)["count"]
+    assert call.run(*args)["count"] == c["count"]
+
+
 def test_plugin_errors(gpu):
     call = gpu.PluginCall(np.zeros(2), np.array([[1.0, 2.0], [2.0, 1.0]]))
     assert call.run(1000, 1, 0.02, 1)["status"] == -1
