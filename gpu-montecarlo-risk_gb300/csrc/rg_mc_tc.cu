@@ -2,14 +2,14 @@
 //
 // Computes what the plain kernels compute (R = H mu + L Zsum per path, S,
 // w.R, crash / breach / VaR bookkeeping) with the contraction as a dense
-// MMA on sm_103a tensor cores, in transposed form so that a whole path
-// tile's normals fit on chip:
+// MMA on sm_103a tensor cores, in transposed form so that a path tile's
+// normals fit on chip:
 //
 //     D[asset, path] = sum_k Lhat[asset, k] * Z[path, k]      (tcgen05.mma)
 //
-// M = 128 asset rows per MMA (n_mt = ceil((N+1)/128) row tiles), N = 64 paths
+// M = 128 asset rows per MMA (n_mt = ceil((N+1)/128) row tiles), N = P paths
 // per tile, K = 16 per instruction, FP32 accumulators in tensor memory
-// (n_mt x 64 columns, <= 512).  Row N of Lhat is w^T L, so the portfolio
+// (n_mt x P columns, <= 512).  Row N of Lhat is w^T L, so the portfolio
 // return w.R = H w.mu + D[N, path] comes out of the same MMAs.
 //
 // Precision: both operands are split into FP16 (or BF16) hi + lo parts and
@@ -17,20 +17,19 @@
 // is below FP32 rounding for FP16).  L is scaled by 2^8 so its lo part stays
 // in FP16's normal range; the epilogue scales back exactly.
 //
-// Per CTA (one per SM, persistent over 64-path tiles):
-//   1. all 512 threads draw the tile's normals (engine Philox layout, summed
-//      over H days, or one sqrt(H)-scaled draw per asset in the aggregated
-//      mode), split them and store them in shared memory in the canonical
-//      K-major 128-byte-swizzled layout (one 64 x 64 block per K tile);
-//   2. one thread of warp 1 streams the pre-swizzled Lhat tiles (128 x 64,
-//      hi and lo, 32 KB) from HBM with cp.async.bulk into a 2-stage ring
-//      guarded by mbarriers; one thread of warp 0 issues the MMAs for each
-//      row tile over its K tiles (lower triangle: row tile m needs
-//      K < 128 (m + 1)) and commits each stage back to the producer;
-//   3. all 16 warps read the accumulators with tcgen05.ld (warp w reads
-//      lanes 32 (w % 4) .. +31 and a quarter of the columns), compare each
-//      asset's return with -x (ballot + popc per path) and collect w.R from
-//      row N.
+// Two kernels, one CTA per SM, persistent over path tiles:
+//   mc_tcws_kernel   (the engine's default) warp-specialised, 1024 threads:
+//                    26 generator warps draw the next tile's normals into a
+//                    ring of K-tile slots while one thread streams the
+//                    pre-swizzled Lhat tiles (cp.async.bulk, mbarrier ring),
+//                    one thread issues the MMAs K-tile-outer, and four warps
+//                    read each row tile's accumulators (tcgen05.ld) as soon
+//                    as it is complete.  P = 96 paths where tensor memory
+//                    allows (N <= 639), else 64.
+//   mc_tc_kernel     phase-serial, 512 threads, P = 64: all threads draw the
+//                    tile's normals, one thread streams Lhat through a
+//                    2-stage ring while another issues the MMAs row tile by
+//                    row tile, then all 16 warps read the accumulators.
 // Every wait is bounded: on expiry the kernel sets an error word, drains its
 // own copies and MMAs (again bounded), frees its tensor memory and returns;
 // the host reports RG_ERR_TIMEOUT.
