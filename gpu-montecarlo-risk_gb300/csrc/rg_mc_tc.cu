@@ -571,17 +571,18 @@ static constexpr int kWsProdWarp = 5;
 static constexpr int kWsGenWarp0 = 6;
 static constexpr int kWsGenThreads = kWsThreads - 32 * kWsGenWarp0;
 static constexpr int kTcMaxMt = (kTcMaxKt * kTcKt + 1 + kTcRows - 1) / kTcRows;
-static constexpr int kWsZSlots = 4; // K-tile slots of Z (hi + lo, P x 64 x 2 bytes each part)
-
-// Paths per tile P (the MMA's N): 96 when the item's row tiles fit in tensor
-// memory at that width (n_mt x 96 <= 512 columns, N <= 639), else 64.  A
-// 96-path tile moves 7 KB of operands per 1.5x the work of a 64-path MMA
-// (6 KB) and streams each Lhat tile once per 96 paths; its Z ring (96 KB)
-// leaves room for 4 Lhat stages, the 64-path form's (64 KB) for 5.
+// Paths per tile P (the MMA's N): the widest of 128, 96, 64 at which the
+// item's row tiles fit in tensor memory (n_mt x P <= 512 columns: P = 128 up
+// to N = 511, 96 up to N = 639).  A wider tile moves fewer operand bytes per
+// MMA flop (7 KB per 1.5x the work of a 64-path MMA at P = 96, 8 KB per 2x
+// at 128), streams each Lhat tile once per P paths and issues fewer MMAs per
+// path.  Shared memory: Z ring (kZSlots K-tile slots, hi + lo) + Lhat ring
+// (kStages x 32 KB) + alignment = 230.4 KB for every P.
 template <int P> struct WsShape {
     static constexpr int kZBytes = P * kTcKt * 2;          // one part of a Z K tile
+    static constexpr int kZSlots = (P == 128) ? 3 : 4;     // K-tile slots of Z
     static constexpr int kStages = (P == 64) ? 5 : 4;      // Lhat ring stages (hi + lo, 32 KB each)
-    static constexpr size_t kSmem = 1024 + (size_t)kWsZSlots * 2 * kZBytes + (size_t)kStages * 2 * kTcTileBytes;
+    static constexpr size_t kSmem = 1024 + (size_t)kZSlots * 2 * kZBytes + (size_t)kStages * 2 * kTcTileBytes;
     static_assert(P % 16 == 0 && P >= 64 && P <= 128, "path tile");
     static_assert(kSmem <= 227 * 1024 - 2048, "shared memory");
 };
@@ -614,7 +615,7 @@ template <bool VAR, bool BATCH, int P>
 __global__ void __launch_bounds__(kWsThreads, 1) mc_tcws_kernel(const __grid_constant__ TcBatch b)
 {
     using Sh = WsShape<P>;
-    constexpr int kStages = Sh::kStages, kZB = Sh::kZBytes;
+    constexpr int kStages = Sh::kStages, kZB = Sh::kZBytes, kWsZSlots = Sh::kZSlots;
     extern __shared__ __align__(1024) unsigned char tc_smem[];
     const PlainArgs &a = b.var;
     unsigned char *base = (unsigned char *)(((uintptr_t)tc_smem + 1023) & ~(uintptr_t)1023);
@@ -1058,7 +1059,7 @@ static size_t tc_smem_bytes(int n_kt_max)
 
 // Paths per tile of the warp-specialised kernel for items of at most
 // n_mt_max row tiles (tensor memory holds n_mt x paths FP32 columns).
-int tc_batch_paths(int n_mt_max) { return n_mt_max * 96 <= 512 ? 96 : 64; }
+int tc_batch_paths(int n_mt_max) { return n_mt_max * 128 <= 512 ? 128 : (n_mt_max * 96 <= 512 ? 96 : 64); }
 
 static void fill_item(TcItem &it, const PlainArgs &a, const unsigned char *tiles, int bf16, bool aggregated,
                       double wmu, long long tile_begin)
@@ -1112,15 +1113,17 @@ cudaError_t launch_tc(const PlainArgs &a, const unsigned char *tiles, int bf16, 
     b.inject_stall = inject_stall ? 1 : 0;
     b.n_kt_max = b.one.n_kt;
     b.var = a;
-    // The warp-specialised kernel (96-path tiles where tensor memory allows,
-    // else 64): generation, MMAs and the per-row-tile epilogue overlap.
+    // The warp-specialised kernel (the widest path tile tensor memory
+    // allows): generation, MMAs and the per-row-tile epilogue overlap.
     // RG_TC_KERNEL=simple selects the phase-serial kernel (64-path tiles:
     // generate, multiply, read back in turn), kept as a second
-    // implementation that the tests compare; RG_TC_KERNEL=ws64 forces the
-    // warp-specialised kernel's 64-path form.
+    // implementation that the tests compare; RG_TC_KERNEL=ws64 / ws96 cap
+    // the warp-specialised kernel's tile at 64 / 96 paths.
     const char *sel = getenv("RG_TC_KERNEL");
     const bool simple = sel && strstr(sel, "simple");
-    const int paths = simple || (sel && strstr(sel, "ws64")) ? 64 : tc_batch_paths(b.one.n_mt);
+    int paths = simple ? 64 : tc_batch_paths(b.one.n_mt);
+    if (sel && strstr(sel, "ws64")) paths = 64;
+    if (sel && strstr(sel, "ws96") && paths > 96) paths = 96;
     b.total_tiles = (a.n_paths + paths - 1) / paths;
     b.tmem_cols = tmem_cols_for(b.one.n_mt, paths);
     if (b.one.n_mt * paths > 512) return cudaErrorInvalidValue;
@@ -1130,6 +1133,9 @@ cudaError_t launch_tc(const PlainArgs &a, const unsigned char *tiles, int bf16, 
     if (simple)
         return var ? launch_one(mc_tc_kernel<true, false>, b, kTcThreads, tc_smem_bytes(b.n_kt_max), grid, s)
                    : launch_one(mc_tc_kernel<false, false>, b, kTcThreads, tc_smem_bytes(b.n_kt_max), grid, s);
+    if (paths == 128)
+        return var ? launch_one(mc_tcws_kernel<true, false, 128>, b, kWsThreads, WsShape<128>::kSmem, grid, s)
+                   : launch_one(mc_tcws_kernel<false, false, 128>, b, kWsThreads, WsShape<128>::kSmem, grid, s);
     if (paths == 96)
         return var ? launch_one(mc_tcws_kernel<true, false, 96>, b, kWsThreads, WsShape<96>::kSmem, grid, s)
                    : launch_one(mc_tcws_kernel<false, false, 96>, b, kWsThreads, WsShape<96>::kSmem, grid, s);
@@ -1170,7 +1176,9 @@ cudaError_t launch_tc_batch(const void *d_items, int n_items, long long total_ti
     const int paths = tc_batch_paths(n_mt_max);
     b.tmem_cols = tmem_cols_for(n_mt_max, paths);
     if (n_mt_max * paths > 512 || n_kt_max > kTcMaxKt) return cudaErrorInvalidValue;
-    if (paths == 96)
+    if (paths == 128)
+        mc_tcws_kernel<false, true, 128><<<(unsigned)grid, kWsThreads, WsShape<128>::kSmem, s>>>(b);
+    else if (paths == 96)
         mc_tcws_kernel<false, true, 96><<<(unsigned)grid, kWsThreads, WsShape<96>::kSmem, s>>>(b);
     else
         mc_tcws_kernel<false, true, 64><<<(unsigned)grid, kWsThreads, WsShape<64>::kSmem, s>>>(b);
@@ -1183,12 +1191,14 @@ cudaError_t launch_tc_batch(const void *d_items, int n_items, long long total_ti
 int tc_batch_occupancy(int n_mt_max)
 {
     int per_sm = 0;
+    const int paths = tc_batch_paths(n_mt_max);
     const cudaError_t e =
-        tc_batch_paths(n_mt_max) == 96
-            ? cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, mc_tcws_kernel<false, true, 96>, kWsThreads,
-                                                            WsShape<96>::kSmem)
-            : cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, mc_tcws_kernel<false, true, 64>, kWsThreads,
-                                                            WsShape<64>::kSmem);
+        paths == 128 ? cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, mc_tcws_kernel<false, true, 128>,
+                                                                     kWsThreads, WsShape<128>::kSmem)
+        : paths == 96 ? cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, mc_tcws_kernel<false, true, 96>,
+                                                                      kWsThreads, WsShape<96>::kSmem)
+                      : cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, mc_tcws_kernel<false, true, 64>,
+                                                                      kWsThreads, WsShape<64>::kSmem);
     if (e != cudaSuccess) return 1;
     return per_sm < 1 ? 1 : per_sm;
 }
@@ -1197,8 +1207,11 @@ int tc_batch_occupancy(int n_mt_max)
 // before any launch or capture.
 cudaError_t tc_batch_prepare()
 {
-    cudaError_t e = cudaFuncSetAttribute(mc_tcws_kernel<false, true, 96>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                         (int)WsShape<96>::kSmem);
+    cudaError_t e = cudaFuncSetAttribute(mc_tcws_kernel<false, true, 128>,
+                                         cudaFuncAttributeMaxDynamicSharedMemorySize, (int)WsShape<128>::kSmem);
+    if (e == cudaSuccess)
+        e = cudaFuncSetAttribute(mc_tcws_kernel<false, true, 96>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                 (int)WsShape<96>::kSmem);
     if (e == cudaSuccess)
         e = cudaFuncSetAttribute(mc_tcws_kernel<false, true, 64>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                  (int)WsShape<64>::kSmem);

@@ -36,10 +36,11 @@ def _case(n, seed):
     return mu, sigma, w
 
 
-# the tcgen05 kernels: "ws" (warp-specialised, the default: 96-path tiles up
-# to five row tiles, N <= 639), "ws64" (its 64-path form) and "simple"
-# (phase-serial, 64-path tiles); RG_TC_KERNEL forces one of them
-KERNELS = ["ws", "ws64", "simple"]
+# the tcgen05 kernels: "ws" (warp-specialised, the default: 128-path tiles up
+# to four row tiles, N <= 511; 96 up to five, N <= 639; else 64), "ws96" and
+# "ws64" (its tile capped at 96 / 64 paths) and "simple" (phase-serial,
+# 64-path tiles); RG_TC_KERNEL forces one of them
+KERNELS = ["ws", "ws96", "ws64", "simple"]
 
 
 @pytest.mark.parametrize("kernel", KERNELS)
