@@ -24,8 +24,8 @@
 //                    pre-swizzled Lhat tiles (cp.async.bulk, mbarrier ring),
 //                    one thread issues the MMAs K-tile-outer, and four warps
 //                    read each row tile's accumulators (tcgen05.ld) as soon
-//                    as it is complete.  P = 96 paths where tensor memory
-//                    allows (N <= 639), else 64.
+//                    as it is complete.  P = 128 paths up to N = 511, 96
+//                    up to N = 639, else 64 (tensor-memory columns).
 //   mc_tc_kernel     phase-serial, 512 threads, P = 64: all threads draw the
 //                    tile's normals, one thread streams Lhat through a
 //                    2-stage ring while another issues the MMAs row tile by
