@@ -45,8 +45,8 @@ KERNELS = ["ws", "ws96", "ws64", "simple"]
 
 @pytest.mark.parametrize("kernel", KERNELS)
 @pytest.mark.parametrize("prec", ["fp16x3", "bf16x3"])
-@pytest.mark.parametrize("n,horizon,M", [(1, 1, 300), (16, 1, 256), (64, 1, 1000), (130, 2, 777), (600, 10, 256),
-                                         (640, 2, 200)])
+@pytest.mark.parametrize("n,horizon,M", [(1, 1, 300), (16, 1, 256), (64, 1, 1000), (130, 2, 777), (511, 1, 300),
+                                         (512, 1, 300), (600, 10, 256), (639, 1, 200), (640, 2, 200)])
 def test_tc_per_path_parity(gpu, oracle, monkeypatch, kernel, prec, n, horizon, M):
     monkeypatch.setenv("RG_TC_KERNEL", kernel)
     code, near_tol, port_tol = CASES[prec]
