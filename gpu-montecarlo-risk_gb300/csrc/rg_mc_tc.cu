@@ -124,6 +124,18 @@ __device__ __forceinline__ bool mbar_try_wait(uint64_t *bar, unsigned parity)
                  : "memory");
     return ok != 0;
 }
+// Non-blocking probe of a phase (mbarrier.test_wait never suspends).
+__device__ __forceinline__ bool mbar_test(uint64_t *bar, unsigned parity)
+{
+    uint32_t ok;
+    asm volatile("{\n\t.reg .pred p;\n\t"
+                 "mbarrier.test_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+                 "selp.u32 %0, 1, 0, p;\n\t}"
+                 : "=r"(ok)
+                 : "r"(smem_u32(bar)), "r"(parity)
+                 : "memory");
+    return ok != 0;
+}
 __device__ __forceinline__ unsigned long long global_ns()
 {
     unsigned long long t;
@@ -533,20 +545,21 @@ __global__ void __launch_bounds__(kTcThreads, 1) mc_tc_kernel(const __grid_const
 }
 
 // ----------------------------------------------------------------------
-// Warp-specialised form of the same computation.  1024 threads, four roles:
+// Warp-specialised form of the same computation.  1024 threads, three roles:
 //   warps 0-3    epilogue: warp w reads TMEM lanes 32 w .. +31 of a row tile
 //                as soon as that row tile is fully accumulated;
-//   warp 4       lane 0 issues the MMAs;
-//   warp 5       lane 0 streams the Lhat tiles into the ring;
-//   warps 6-31   (832 threads) generator: draws the normals one 64-column K
-//                tile at a time into a ring of kWsZSlots K-tile slots.
+//   warp 4       lane 0 streams the Lhat tiles into the ring (bulk copies,
+//                issued between MMA pairs whenever a stage is free) and
+//                issues the MMAs;
+//   warps 5-31   (864 threads) generator: draws the normals one 64-column K
+//                tile at a time into a ring of K-tile slots.
 // The MMAs run K-tile-outer (for each K tile, every row tile that needs it),
 // so a K tile is needed only while its MMAs run: K tiles are numbered in
-// order across the CTA's path tiles (g), K tile g lives in slot g % kWsZSlots
-// and the slot is released (zempty) as soon as its MMAs complete.  A ring of
-// four slots (64 KB) instead of a whole path tile's normals (160 KB) leaves
-// room for a five-stage Lhat ring, which hides the L2 latency of the copies.  Row tile
-// m is complete after K tile kts(m) - 1 (lower triangle), so its epilogue runs
+// order across the CTA's path tiles (g), K tile g lives in slot g % kZSlots
+// and the slot is released (zempty) as soon as its MMAs complete; a few
+// slots instead of a whole path tile's normals leave room for a 4-5 stage
+// Lhat ring, which hides the L2 latency of the copies.  Row tile m is
+// complete after K tile kts(m) - 1 (lower triangle), so its epilogue runs
 // while later K tiles are still being drawn, and the next tile's MMAs
 // overwrite its accumulator once the epilogue has read it (acc_free): only
 // the last row tile's epilogue is on the critical path.
@@ -555,21 +568,18 @@ __global__ void __launch_bounds__(kTcThreads, 1) mc_tc_kernel(const __grid_const
 //   zfull[z]     generator -> MMA: the K tile in slot z written (one arrival
 //                per generator thread)
 //   zempty[z]    MMA -> generator: the MMAs that read slot z are complete
-//   full/empty   Lhat ring between producer and MMA issuer
+//   full/empty   Lhat ring (copy completion, MMA completion)
 //   acc_full[m]  MMA -> epilogue: row tile m of the tile accumulated
 //   acc_free[m]  epilogue -> MMA: row tile m read (one arrival per warp)
 //   slot_free[s] epilogue -> generator: the tile in slot s is finished
 // The K-tile number g, use counts per row tile and per item slot (the same
 // on both sides of each barrier) give the phase parities, since items of a
-// batch differ in size.  The tile index is read after tile_pub, never after zfull[0]: slot s
-// is republished only after the epilogue finished the tile that used it, so
-// no waiter can fall a whole phase behind.
+// batch differ in size.  The tile index is read after tile_pub, never after
+// zfull[0]: slot s is republished only after the epilogue finished the tile
+// that used it, so no waiter can fall a whole phase behind.
 static constexpr int kWsThreads = 1024;
 static constexpr int kWsEpiWarps = 4;
 static constexpr int kWsMmaWarp = 4;
-static constexpr int kWsProdWarp = 5;
-static constexpr int kWsGenWarp0 = 6;
-static constexpr int kWsGenThreads = kWsThreads - 32 * kWsGenWarp0;
 static constexpr int kTcMaxMt = (kTcMaxKt * kTcKt + 1 + kTcRows - 1) / kTcRows;
 // Paths per tile P (the MMA's N): the widest of 128, 96, 64 at which the
 // item's row tiles fit in tensor memory (n_mt x P <= 512 columns: P = 128 up
@@ -611,11 +621,16 @@ __device__ __forceinline__ int tc_kts(int mt, int n_mt, int n_kt)
     return (mt == n_mt - 1) ? n_kt : min(n_kt, (kTcRows * (mt + 1) + kTcKt - 1) / kTcKt);
 }
 
-template <bool VAR, bool BATCH, int P>
+template <bool VAR, bool BATCH, int P, bool SPLIT>
 __global__ void __launch_bounds__(kWsThreads, 1) mc_tcws_kernel(const __grid_constant__ TcBatch b)
 {
     using Sh = WsShape<P>;
     constexpr int kStages = Sh::kStages, kZB = Sh::kZBytes, kWsZSlots = Sh::kZSlots;
+    // SPLIT: warp 5 streams the Lhat tiles (when the MMAs bound the kernel,
+    // refills never wait for the MMA thread); otherwise the MMA thread
+    // issues the copies too and warp 5 draws normals
+    constexpr int kWsGenWarp0 = SPLIT ? 6 : 5;
+    constexpr int kWsGenThreads = kWsThreads - 32 * kWsGenWarp0;
     extern __shared__ __align__(1024) unsigned char tc_smem[];
     const PlainArgs &a = b.var;
     unsigned char *base = (unsigned char *)(((uintptr_t)tc_smem + 1023) & ~(uintptr_t)1023);
@@ -789,7 +804,7 @@ __global__ void __launch_bounds__(kWsThreads, 1) mc_tcws_kernel(const __grid_con
             }
             g0 += (unsigned)n_kt;
         }
-    } else if (warp == kWsProdWarp) {
+    } else if (SPLIT && warp == kWsMmaWarp + 1) {
         // ======================= Lhat producer =======================
         if (lane == 0) {
             unsigned prod_iter = 0;
@@ -832,10 +847,74 @@ __global__ void __launch_bounds__(kWsThreads, 1) mc_tcws_kernel(const __grid_con
         }
         __syncwarp();
     } else if (warp == kWsMmaWarp) {
-        // ======================= MMA issuer =======================
+        // ============ MMA issue (and, unless SPLIT, the Lhat copies) ============
+        // Pairs (row tile, K tile) are numbered in consumption order across
+        // tiles: pi copies issued, ci pairs multiplied.  pump() issues copies
+        // while the ring has room, probing its barriers without blocking; it
+        // blocks only when the next pair to multiply has no copy yet (need).
+        // The copy cursor enters a tile only once that tile is published.
         if (lane == 0) {
+            unsigned pi = 0, ci = 0;
+            int skipped = -1;             // the pair left unfilled by the fault injection
+            unsigned pj = 0;              // tile (sequence number) of the copy cursor
+            bool p_live = false, p_end = false;
+            int pkt = 0, pmt = 0, p_nkt = 0, p_nmt = 0;
+            const unsigned char *p_tiles = nullptr;
+            auto pump = [&](bool need) -> bool {
+                while (!p_end && pi < ci + kStages) {
+                    const bool must = need && pi == ci;
+                    if (!p_live) {
+                        const int ps = (int)(pj & 1u);
+                        const unsigned par = (pj >> 1) & 1u;
+                        if (!mbar_test(&tile_pub[ps], par)) {
+                            if (!must) return true;
+                            if (!mbar_wait(&tile_pub[ps], par)) return false;
+                        }
+                        if (s_tile[ps] < 0) {
+                            p_end = true;
+                            return true;
+                        }
+                        const TcItem &pit = BATCH ? s_item[ps] : b.one;
+                        p_nkt = pit.n_kt;
+                        p_nmt = pit.n_mt;
+                        p_tiles = pit.tiles;
+                        pkt = 0;
+                        pmt = 0; // (K tile 0, row tile 0) is always a pair
+                        p_live = true;
+                    }
+                    const int st = (int)(pi % kStages);
+                    const unsigned eph = ((pi / kStages) & 1u) ^ 1u;
+                    if (!mbar_test(&empty_bar[st], eph)) {
+                        if (!must) return true;
+                        if (!mbar_wait(&empty_bar[st], eph)) return false;
+                    }
+                    if (b.inject_stall && pi == 1) { // never filled: the MMA side's wait runs out
+                        skipped = (int)pi;
+                    } else {
+                        mbar_expect_tx(&full_bar[st], 2 * kTcTileBytes);
+                        const unsigned char *src = p_tiles + ((size_t)(pmt * p_nkt + pkt) * 2) * kTcTileBytes;
+                        unsigned char *dst = lst + (size_t)st * 2 * kTcTileBytes;
+                        bulk_copy(dst, src, kTcTileBytes, &full_bar[st]);
+                        bulk_copy(dst + kTcTileBytes, src + kTcTileBytes, kTcTileBytes, &full_bar[st]);
+                    }
+                    pi++;
+                    // next pair: row tiles that need K tile pkt form a suffix of 0..n_mt-1
+                    do {
+                        if (++pmt == p_nmt) {
+                            pmt = 0;
+                            ++pkt;
+                        }
+                    } while (pkt < p_nkt && pkt >= tc_kts(pmt, p_nmt, p_nkt));
+                    if (pkt == p_nkt) {
+                        p_live = false;
+                        pj++;
+                    }
+                }
+                return true;
+            };
+
             unsigned g0 = 0, fpar = 0; // fpar bit m: parity of the uses of row tile m
-            unsigned rs = 0, rph = 0;  // Lhat ring: stage and phase parity of the next pair
+            unsigned rs = 0, rph = 0;  // Lhat ring: stage and phase parity of pair ci
             const uint32_t lst_lo = sw128_desc_lo(smem_u32(lst));
             for (unsigned j = 0; !tm_abort; j++) {
                 const int slot = j & 1;
@@ -851,7 +930,7 @@ __global__ void __launch_bounds__(kWsThreads, 1) mc_tcws_kernel(const __grid_con
                 for (int kt = 0; kt < n_kt && !tm_abort; kt++) {
                     const unsigned g = g0 + (unsigned)kt;
                     const int zs = (int)(g % kWsZSlots);
-                    if (!mbar_wait(&zfull[zs], (g / kWsZSlots) & 1u)) {
+                    if ((!SPLIT && !pump(false)) || !mbar_wait(&zfull[zs], (g / kWsZSlots) & 1u)) {
                         atomicOr(b.err, 64u);
                         tm_abort = 1;
                         break;
@@ -868,6 +947,11 @@ __global__ void __launch_bounds__(kWsThreads, 1) mc_tcws_kernel(const __grid_con
                             tm_abort = 1;
                             break;
                         }
+                        if (!SPLIT && !pump(true)) {
+                            atomicOr(b.err, 1u);
+                            tm_abort = 1;
+                            break;
+                        }
                         if (!mbar_wait(&full_bar[rs], rph)) {
                             atomicOr(b.err, 2u);
                             tm_abort = 1;
@@ -877,6 +961,7 @@ __global__ void __launch_bounds__(kWsThreads, 1) mc_tcws_kernel(const __grid_con
                         tc_mma_pair(tmem + (uint32_t)(mt * P), lst_lo + (uint32_t)rs * (2 * kTcTileBytes >> 4),
                                     zh_lo, zl_lo, idesc, kt > 0 ? 1u : 0u);
                         tc_commit(&empty_bar[rs]);
+                        ci++;
                         if (++rs == kStages) {
                             rs = 0;
                             rph ^= 1u;
@@ -888,8 +973,13 @@ __global__ void __launch_bounds__(kWsThreads, 1) mc_tcws_kernel(const __grid_con
                 g0 += (unsigned)n_kt;
                 fpar ^= (1u << n_mt) - 1u;
             }
-            // every MMA issued (and every commit's arrival) completes before
-            // the tensor memory and the barriers are released
+            // copies issued but not multiplied (only after an abort) land
+            // before the kernel ends; every MMA issued (and every commit's
+            // arrival) completes before the tensor memory and the barriers
+            // are released
+            if (!SPLIT)
+                for (unsigned i = ci; i < pi; i++)
+                    if ((int)i != skipped) mbar_wait(&full_bar[i % kStages], (i / kStages) & 1u);
             tc_commit(&drain_bar);
             mbar_wait(&drain_bar, 0u);
         }
@@ -1114,16 +1204,21 @@ cudaError_t launch_tc(const PlainArgs &a, const unsigned char *tiles, int bf16, 
     b.n_kt_max = b.one.n_kt;
     b.var = a;
     // The warp-specialised kernel (the widest path tile tensor memory
-    // allows): generation, MMAs and the per-row-tile epilogue overlap.
-    // RG_TC_KERNEL=simple selects the phase-serial kernel (64-path tiles:
-    // generate, multiply, read back in turn), kept as a second
-    // implementation that the tests compare; RG_TC_KERNEL=ws64 / ws96 cap
-    // the warp-specialised kernel's tile at 64 / 96 paths.
+    // allows): generation, MMAs and the per-row-tile epilogue overlap.  With
+    // daily draws the normals bound it, and the MMA thread also issues the
+    // Lhat copies (one more generator warp); with aggregated draws the MMAs
+    // bound it, and a separate warp streams the copies (SPLIT).
+    // RG_TC_KERNEL overrides: "simple" the phase-serial kernel (64-path
+    // tiles, kept as a second implementation that the tests compare),
+    // "ws64" / "ws96" cap the tile, "split" / "merged" force the copy issuer.
     const char *sel = getenv("RG_TC_KERNEL");
     const bool simple = sel && strstr(sel, "simple");
     int paths = simple ? 64 : tc_batch_paths(b.one.n_mt);
     if (sel && strstr(sel, "ws64")) paths = 64;
     if (sel && strstr(sel, "ws96") && paths > 96) paths = 96;
+    bool split = aggregated;
+    if (sel && strstr(sel, "split")) split = true;
+    if (sel && strstr(sel, "merged")) split = false;
     b.total_tiles = (a.n_paths + paths - 1) / paths;
     b.tmem_cols = tmem_cols_for(b.one.n_mt, paths);
     if (b.one.n_mt * paths > 512) return cudaErrorInvalidValue;
@@ -1133,14 +1228,20 @@ cudaError_t launch_tc(const PlainArgs &a, const unsigned char *tiles, int bf16, 
     if (simple)
         return var ? launch_one(mc_tc_kernel<true, false>, b, kTcThreads, tc_smem_bytes(b.n_kt_max), grid, s)
                    : launch_one(mc_tc_kernel<false, false>, b, kTcThreads, tc_smem_bytes(b.n_kt_max), grid, s);
-    if (paths == 128)
-        return var ? launch_one(mc_tcws_kernel<true, false, 128>, b, kWsThreads, WsShape<128>::kSmem, grid, s)
-                   : launch_one(mc_tcws_kernel<false, false, 128>, b, kWsThreads, WsShape<128>::kSmem, grid, s);
-    if (paths == 96)
-        return var ? launch_one(mc_tcws_kernel<true, false, 96>, b, kWsThreads, WsShape<96>::kSmem, grid, s)
-                   : launch_one(mc_tcws_kernel<false, false, 96>, b, kWsThreads, WsShape<96>::kSmem, grid, s);
-    return var ? launch_one(mc_tcws_kernel<true, false, 64>, b, kWsThreads, WsShape<64>::kSmem, grid, s)
-               : launch_one(mc_tcws_kernel<false, false, 64>, b, kWsThreads, WsShape<64>::kSmem, grid, s);
+#define RG_WS_LAUNCH(PP, SS)                                                                                      \
+    return var ? launch_one(mc_tcws_kernel<true, false, PP, SS>, b, kWsThreads, WsShape<PP>::kSmem, grid, s)     \
+               : launch_one(mc_tcws_kernel<false, false, PP, SS>, b, kWsThreads, WsShape<PP>::kSmem, grid, s)
+    if (paths == 128) {
+        if (split) RG_WS_LAUNCH(128, true);
+        RG_WS_LAUNCH(128, false);
+    }
+    if (paths == 96) {
+        if (split) RG_WS_LAUNCH(96, true);
+        RG_WS_LAUNCH(96, false);
+    }
+    if (split) RG_WS_LAUNCH(64, true);
+    RG_WS_LAUNCH(64, false);
+#undef RG_WS_LAUNCH
 }
 
 // Host-side description of one batch item for tc_batch_items.
@@ -1177,11 +1278,11 @@ cudaError_t launch_tc_batch(const void *d_items, int n_items, long long total_ti
     b.tmem_cols = tmem_cols_for(n_mt_max, paths);
     if (n_mt_max * paths > 512 || n_kt_max > kTcMaxKt) return cudaErrorInvalidValue;
     if (paths == 128)
-        mc_tcws_kernel<false, true, 128><<<(unsigned)grid, kWsThreads, WsShape<128>::kSmem, s>>>(b);
+        mc_tcws_kernel<false, true, 128, false><<<(unsigned)grid, kWsThreads, WsShape<128>::kSmem, s>>>(b);
     else if (paths == 96)
-        mc_tcws_kernel<false, true, 96><<<(unsigned)grid, kWsThreads, WsShape<96>::kSmem, s>>>(b);
+        mc_tcws_kernel<false, true, 96, false><<<(unsigned)grid, kWsThreads, WsShape<96>::kSmem, s>>>(b);
     else
-        mc_tcws_kernel<false, true, 64><<<(unsigned)grid, kWsThreads, WsShape<64>::kSmem, s>>>(b);
+        mc_tcws_kernel<false, true, 64, false><<<(unsigned)grid, kWsThreads, WsShape<64>::kSmem, s>>>(b);
     return cudaGetLastError();
 }
 
@@ -1193,11 +1294,11 @@ int tc_batch_occupancy(int n_mt_max)
     int per_sm = 0;
     const int paths = tc_batch_paths(n_mt_max);
     const cudaError_t e =
-        paths == 128 ? cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, mc_tcws_kernel<false, true, 128>,
+        paths == 128 ? cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, mc_tcws_kernel<false, true, 128, false>,
                                                                      kWsThreads, WsShape<128>::kSmem)
-        : paths == 96 ? cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, mc_tcws_kernel<false, true, 96>,
+        : paths == 96 ? cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, mc_tcws_kernel<false, true, 96, false>,
                                                                       kWsThreads, WsShape<96>::kSmem)
-                      : cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, mc_tcws_kernel<false, true, 64>,
+                      : cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, mc_tcws_kernel<false, true, 64, false>,
                                                                       kWsThreads, WsShape<64>::kSmem);
     if (e != cudaSuccess) return 1;
     return per_sm < 1 ? 1 : per_sm;
@@ -1207,13 +1308,13 @@ int tc_batch_occupancy(int n_mt_max)
 // before any launch or capture.
 cudaError_t tc_batch_prepare()
 {
-    cudaError_t e = cudaFuncSetAttribute(mc_tcws_kernel<false, true, 128>,
+    cudaError_t e = cudaFuncSetAttribute(mc_tcws_kernel<false, true, 128, false>,
                                          cudaFuncAttributeMaxDynamicSharedMemorySize, (int)WsShape<128>::kSmem);
     if (e == cudaSuccess)
-        e = cudaFuncSetAttribute(mc_tcws_kernel<false, true, 96>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+        e = cudaFuncSetAttribute(mc_tcws_kernel<false, true, 96, false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                  (int)WsShape<96>::kSmem);
     if (e == cudaSuccess)
-        e = cudaFuncSetAttribute(mc_tcws_kernel<false, true, 64>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+        e = cudaFuncSetAttribute(mc_tcws_kernel<false, true, 64, false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                  (int)WsShape<64>::kSmem);
     return e;
 }

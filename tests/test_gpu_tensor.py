@@ -37,10 +37,12 @@ def _case(n, seed):
 
 
 # the tcgen05 kernels: "ws" (warp-specialised, the default: 128-path tiles up
-# to four row tiles, N <= 511; 96 up to five, N <= 639; else 64), "ws96" and
-# "ws64" (its tile capped at 96 / 64 paths) and "simple" (phase-serial,
-# 64-path tiles); RG_TC_KERNEL forces one of them
-KERNELS = ["ws", "ws96", "ws64", "simple"]
+# to four row tiles, N <= 511; 96 up to five, N <= 639; else 64; the Lhat
+# copies issued by their own warp with aggregated draws, by the MMA thread
+# with daily draws), "ws-split" / "ws-merged" (either copy issuer forced),
+# "ws96" and "ws64" (its tile capped at 96 / 64 paths) and "simple"
+# (phase-serial, 64-path tiles); RG_TC_KERNEL forces one of them
+KERNELS = ["ws", "ws-split", "ws-merged", "ws96", "ws64", "simple"]
 
 
 @pytest.mark.parametrize("kernel", KERNELS)
