@@ -545,14 +545,16 @@ __global__ void __launch_bounds__(kTcThreads, 1) mc_tc_kernel(const __grid_const
 }
 
 // ----------------------------------------------------------------------
-// Warp-specialised form of the same computation.  1024 threads, three roles:
+// Warp-specialised form of the same computation.  1024 threads:
 //   warps 0-3    epilogue: warp w reads TMEM lanes 32 w .. +31 of a row tile
 //                as soon as that row tile is fully accumulated;
-//   warp 4       lane 0 streams the Lhat tiles into the ring (bulk copies,
-//                issued between MMA pairs whenever a stage is free) and
-//                issues the MMAs;
-//   warps 5-31   (864 threads) generator: draws the normals one 64-column K
-//                tile at a time into a ring of K-tile slots.
+//   warp 4       lane 0 issues the MMAs and, unless SPLIT, streams the Lhat
+//                tiles into the ring (bulk copies issued between MMA pairs
+//                whenever a stage is free);
+//   warp 5       SPLIT: lane 0 streams the Lhat tiles (used when the MMAs
+//                bound the kernel, so refills never wait for the MMA thread)
+//   warps 5|6-31 (864 | 832 threads) generator: draws the normals one
+//                64-column K tile at a time into a ring of K-tile slots.
 // The MMAs run K-tile-outer (for each K tile, every row tile that needs it),
 // so a K tile is needed only while its MMAs run: K tiles are numbered in
 // order across the CTA's path tiles (g), K tile g lives in slot g % kZSlots
