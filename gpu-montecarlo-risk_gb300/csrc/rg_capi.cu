@@ -125,18 +125,21 @@ static int admit(size_t need)
 static void portfolio_free(Portfolio *p)
 {
     if (!p) return;
-    cudaFree(p->d_L64);
-    cudaFree(p->d_mu64);
-    cudaFree(p->d_Lp);
-    cudaFree(p->d_Lt);
-    cudaFree(p->d_tc[0]);
-    cudaFree(p->d_tc[1]);
-    cudaFree(p->d_err);
-    cudaFree(p->d_w32);
-    cudaFree(p->d_aux);
-    cudaFree(p->d_info);
+    cudaFree(p->d_block);
     delete p;
 }
+
+// Offsets of a portfolio's device buffers inside its one allocation, each
+// aligned to 256 bytes (the tensor tiles are read by bulk copies).
+struct BlockPlan {
+    size_t total = 0;
+    size_t take(size_t bytes)
+    {
+        const size_t at = total;
+        total += (bytes + 255) & ~(size_t)255;
+        return at;
+    }
+};
 
 static int validate_query(const Portfolio *p, const rg_query *q)
 {
@@ -404,23 +407,39 @@ static int create_portfolio(int32_t n, const double *mu, const double *sigma, in
     double aux[2] = {0, 0};
     cudaEvent_t e0 = nullptr, e1 = nullptr;
     cudaStream_t s = ctx->stream;
-    RG_CUDA_TRY(cudaMalloc(&p->d_L64, nn * sizeof(double)));
-    RG_CUDA_TRY(cudaMalloc(&p->d_mu64, (size_t)n * sizeof(double)));
-    RG_CUDA_TRY(cudaMalloc(&p->d_Lp, (size_t)packed_len(n) * sizeof(float)));
-    if (want_lt) RG_CUDA_TRY(cudaMalloc(&p->d_Lt, (size_t)tiled_kpad(n) * tiled_npad(n) * sizeof(float)));
-    RG_CUDA_TRY(cudaMalloc(&p->d_err, sizeof(unsigned int)));
-    if (want_tc[0]) RG_CUDA_TRY(cudaMalloc(&p->d_tc[0], tc_tile_bytes(n)));
-    if (want_tc[1]) RG_CUDA_TRY(cudaMalloc(&p->d_tc[1], tc_tile_bytes(n)));
-    RG_CUDA_TRY(cudaMalloc(&p->d_w32, (size_t)n * sizeof(float)));
-    RG_CUDA_TRY(cudaMalloc(&p->d_aux, (2 + 2 * (size_t)n) * sizeof(double))); // moments + factorisation scratch
-    RG_CUDA_TRY(cudaMalloc(&p->d_info, sizeof(int)));
+    {
+        BlockPlan bp;
+        const size_t oL64 = bp.take(nn * sizeof(double)), omu = bp.take((size_t)n * sizeof(double));
+        const size_t oLp = bp.take((size_t)packed_len(n) * sizeof(float));
+        const size_t oLt = want_lt ? bp.take((size_t)tiled_kpad(n) * tiled_npad(n) * sizeof(float)) : 0;
+        const size_t oerr = bp.take(sizeof(unsigned int));
+        const size_t otc0 = want_tc[0] ? bp.take(tc_tile_bytes(n)) : 0;
+        const size_t otc1 = want_tc[1] ? bp.take(tc_tile_bytes(n)) : 0;
+        const size_t ow32 = bp.take((size_t)n * sizeof(float));
+        const size_t oaux = bp.take((2 + 2 * (size_t)n) * sizeof(double)); // moments + factorisation scratch
+        const size_t oinfo = bp.take(sizeof(int));
+        RG_CUDA_TRY(cudaMalloc(&p->d_block, bp.total));
+        unsigned char *blk = static_cast<unsigned char *>(p->d_block);
+        p->d_L64 = reinterpret_cast<double *>(blk + oL64);
+        p->d_mu64 = reinterpret_cast<double *>(blk + omu);
+        p->d_Lp = reinterpret_cast<float *>(blk + oLp);
+        p->d_Lt = want_lt ? reinterpret_cast<float *>(blk + oLt) : nullptr;
+        p->d_err = reinterpret_cast<unsigned int *>(blk + oerr);
+        p->d_tc[0] = want_tc[0] ? blk + otc0 : nullptr;
+        p->d_tc[1] = want_tc[1] ? blk + otc1 : nullptr;
+        p->d_w32 = reinterpret_cast<float *>(blk + ow32);
+        p->d_aux = reinterpret_cast<double *>(blk + oaux);
+        p->d_info = reinterpret_cast<int *>(blk + oinfo);
+    }
     if (!dev_in) {
-        RG_CUDA_TRY(cudaMalloc(&dA, nn * sizeof(double)));
+        // Sigma and the weights share one upload buffer
+        const size_t a_bytes = (nn * sizeof(double) + 255) & ~(size_t)255;
+        RG_CUDA_TRY(cudaMalloc(&dA, a_bytes + (weights ? (size_t)n * sizeof(double) : 0)));
         RG_CUDA_TRY(cudaMemcpy2DAsync(dA, (size_t)n * sizeof(double), sigma, (size_t)ld * sizeof(double),
                                       (size_t)n * sizeof(double), (size_t)n, cudaMemcpyHostToDevice, s));
         RG_CUDA_TRY(cudaMemcpyAsync(p->d_mu64, mu, (size_t)n * sizeof(double), cudaMemcpyHostToDevice, s));
         if (weights) {
-            RG_CUDA_TRY(cudaMalloc(&dW, (size_t)n * sizeof(double)));
+            dW = reinterpret_cast<double *>(reinterpret_cast<unsigned char *>(dA) + a_bytes);
             RG_CUDA_TRY(cudaMemcpyAsync(dW, weights, (size_t)n * sizeof(double), cudaMemcpyHostToDevice, s));
         }
         A = dA;
@@ -454,15 +473,24 @@ static int create_portfolio(int32_t n, const double *mu, const double *sigma, in
     if (p->d_tc[0]) RG_CUDA_TRY(launch_build_tc_tiles(p->d_L64, p->d_w32, n, 0, p->d_tc[0], s));
     if (p->d_tc[1]) RG_CUDA_TRY(launch_build_tc_tiles(p->d_L64, p->d_w32, n, 1, p->d_tc[1], s));
     RG_CUDA_TRY(cudaMemsetAsync(p->d_err, 0, sizeof(unsigned int), s));
-    RG_CUDA_TRY(cudaStreamSynchronize(s));
+    // host copies for the kernels that take the factor by value: the packed
+    // rows from the device; mu and the FP32 weights from the caller's host
+    // arrays when there are some
     p->h_Lp.resize((size_t)packed_len(n));
     p->h_mu.resize((size_t)n);
     p->h_w.resize((size_t)n);
-    RG_CUDA_TRY(cudaMemcpy(p->h_Lp.data(), p->d_Lp, p->h_Lp.size() * sizeof(float), cudaMemcpyDeviceToHost));
-    RG_CUDA_TRY(cudaMemcpy(p->h_mu.data(), p->d_mu64, (size_t)n * sizeof(double), cudaMemcpyDeviceToHost));
-    RG_CUDA_TRY(cudaMemcpy(p->h_w.data(), p->d_w32, (size_t)n * sizeof(float), cudaMemcpyDeviceToHost));
+    RG_CUDA_TRY(cudaMemcpyAsync(p->h_Lp.data(), p->d_Lp, p->h_Lp.size() * sizeof(float), cudaMemcpyDeviceToHost, s));
+    if (dev_in) {
+        RG_CUDA_TRY(cudaMemcpyAsync(p->h_mu.data(), p->d_mu64, (size_t)n * sizeof(double), cudaMemcpyDeviceToHost, s));
+        RG_CUDA_TRY(cudaMemcpyAsync(p->h_w.data(), p->d_w32, (size_t)n * sizeof(float), cudaMemcpyDeviceToHost, s));
+    } else {
+        for (int i = 0; i < n; i++) {
+            p->h_mu[(size_t)i] = mu[i];
+            p->h_w[(size_t)i] = weights ? (float)weights[i] : 0.f; // as the factorisation writes d_w32
+        }
+    }
+    RG_CUDA_TRY(cudaStreamSynchronize(s));
     cudaFree(dA);
-    cudaFree(dW);
     cudaEventDestroy(e0);
     cudaEventDestroy(e1);
     *out = reinterpret_cast<rg_portfolio *>(p);
@@ -470,7 +498,6 @@ static int create_portfolio(int32_t n, const double *mu, const double *sigma, in
 fail:
     cudaStreamSynchronize(s);
     cudaFree(dA);
-    cudaFree(dW);
     if (e0) cudaEventDestroy(e0);
     if (e1) cudaEventDestroy(e1);
     portfolio_free(p);

@@ -111,6 +111,7 @@ struct Portfolio {
     int n = 0;
     int has_w = 0;
     int device = 0;
+    void *d_block = nullptr;   // one allocation holding every device buffer below
     double *d_L64 = nullptr;   // n x n row-major, zero upper
     double *d_mu64 = nullptr;  // n
     float *d_Lp = nullptr;     // packed rows (packed_len(n) floats)
