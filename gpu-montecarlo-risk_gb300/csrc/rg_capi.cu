@@ -274,8 +274,45 @@ static PlainArgs make_args(const Portfolio *p, const rg_query *q, unsigned long 
     return a;
 }
 
+// A portfolio's buffers live on the device that was current when it was
+// created; its queries run on the current device, so the two must match.
+static int check_device(const Portfolio *p)
+{
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess) {
+        cudaGetLastError();
+        return set_error(RG_ERR_NO_DEVICE, "no CUDA device is available");
+    }
+    if (dev != p->device)
+        return set_error(RG_ERR_INVALID,
+                         "the portfolio was created on device %d but device %d is current: make the "
+                         "portfolio's device current before querying it", p->device, dev);
+    return RG_OK;
+}
+
+// Status of a completed tensor-core pass: the kernel sets its error word
+// when one of its bounded waits ran out, and its counts are then
+// incomplete.  Reads the word on stream s (which it synchronises); RG_OK
+// for the FP32 kernels, which have no such word.
+static int tc_pass_status(const Portfolio *p, const rg_query *q, cudaStream_t s)
+{
+    if (q->precision != RG_PREC_BF16X3 && q->precision != RG_PREC_FP16X3) return RG_OK;
+    unsigned int err = 0;
+    cudaError_t e = cudaMemcpyAsync(&err, p->d_err, sizeof(err), cudaMemcpyDeviceToHost, s);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+    if (e != cudaSuccess)
+        return set_error(RG_ERR_CUDA, "read of the tensor-core error word failed: %s", cudaGetErrorString(e));
+    if (err) return set_error(RG_ERR_TIMEOUT, "tensor-core kernel gave up a bounded wait (error word 0x%x)", err);
+    return RG_OK;
+}
+
 // Shared with rg_noalloc.cu (same checks, same launch selection).
-int query_check(const Portfolio *p, const rg_query *q) { return validate_query(p, q); }
+int query_check(const Portfolio *p, const rg_query *q)
+{
+    const int st = validate_query(p, q);
+    return st ? st : check_device(p);
+}
+int query_pass_status(const Portfolio *p, const rg_query *q, cudaStream_t s) { return tc_pass_status(p, q, s); }
 cudaError_t query_launch(const Portfolio *p, const rg_query *q, const PlainArgs &a, int sm_count,
                          cudaStream_t s)
 {
@@ -538,7 +575,7 @@ int rg_launch_counts(const rg_portfolio *h, const rg_query *q, unsigned long lon
 {
     if (!h || !d_counts) return set_error(RG_ERR_INVALID, "NULL argument");
     const Portfolio *p = reinterpret_cast<const Portfolio *>(h);
-    int st = validate_query(p, q);
+    int st = query_check(p, q);
     if (st) return st;
     DevCtx *ctx;
     st = get_ctx(&ctx, nullptr);
@@ -554,7 +591,7 @@ int rg_simulate(const rg_portfolio *h, const rg_query *q, rg_result *out, void *
 {
     if (!h || !out) return set_error(RG_ERR_INVALID, "NULL argument");
     const Portfolio *p = reinterpret_cast<const Portfolio *>(h);
-    int st = validate_query(p, q);
+    int st = query_check(p, q);
     if (st) return st;
     DevCtx *ctx;
     st = get_ctx(&ctx, nullptr);
@@ -624,14 +661,8 @@ int rg_simulate(const rg_portfolio *h, const rg_query *q, rg_result *out, void *
     RG_CUDA_TRY(cudaStreamSynchronize(s));
     cudaEventElapsedTime(&ms, e0, e1);
     passes = 1;
-    if (q->precision == RG_PREC_BF16X3 || q->precision == RG_PREC_FP16X3) {
-        unsigned int err = 0;
-        RG_CUDA_TRY(cudaMemcpy(&err, p->d_err, sizeof(err), cudaMemcpyDeviceToHost));
-        if (err) {
-            st = set_error(RG_ERR_TIMEOUT, "tensor-core kernel gave up a bounded wait (error word 0x%x)", err);
-            goto fail;
-        }
-    }
+    st = tc_pass_status(p, q, s);
+    if (st) goto fail;
     n_tail = (int64_t)tail[0];
     if (want_var && !(n_tail < T && T <= n_tail + (int64_t)ncand && ncand <= sc.cap)) {
         // The band missed the order statistic: histogram pass over
@@ -648,6 +679,8 @@ int rg_simulate(const rg_portfolio *h, const rg_query *q, rg_result *out, void *
         RG_CUDA_TRY(cudaEventRecord(e1, s));
         RG_CUDA_TRY(cudaMemcpyAsync(hist.data(), sc.hist, hist.size() * 8, cudaMemcpyDeviceToHost, s));
         RG_CUDA_TRY(cudaStreamSynchronize(s));
+        st = tc_pass_status(p, q, s);
+        if (st) goto fail;
         cudaEventElapsedTime(&ms_pass, e0, e1);
         ms += ms_pass;
         int64_t cum = 0;
@@ -682,6 +715,8 @@ int rg_simulate(const rg_portfolio *h, const rg_query *q, rg_result *out, void *
         RG_CUDA_TRY(cudaMemcpyAsync(tail, sc.tail, sizeof(tail), cudaMemcpyDeviceToHost, s));
         RG_CUDA_TRY(cudaMemcpyAsync(&ncand, sc.cand_count, sizeof(ncand), cudaMemcpyDeviceToHost, s));
         RG_CUDA_TRY(cudaStreamSynchronize(s));
+        st = tc_pass_status(p, q, s);
+        if (st) goto fail;
         cudaEventElapsedTime(&ms_pass, e0, e1);
         ms += ms_pass;
         passes = 3;

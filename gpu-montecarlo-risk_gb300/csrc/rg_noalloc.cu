@@ -37,6 +37,7 @@
 namespace rg {
 
 int query_check(const Portfolio *p, const rg_query *q);
+int query_pass_status(const Portfolio *p, const rg_query *q, cudaStream_t s);
 cudaError_t query_launch(const Portfolio *p, const rg_query *q, const PlainArgs &a, int sm_count,
                          cudaStream_t s);
 PlainArgs query_args(const Portfolio *p, const rg_query *q, unsigned long long *d_counts);
@@ -250,6 +251,9 @@ extern "C" int rg_simulate_noalloc(const rg_portfolio *h, const rg_query *q, rg_
     NoAllocHeader hh;
     NA_TRY(cudaMemcpyAsync(&hh, dh, sizeof(hh), cudaMemcpyDeviceToHost, s));
     NA_TRY(cudaStreamSynchronize(s));
+    // a tensor-core pass whose bounded wait ran out left incomplete counts
+    st = query_pass_status(p, q, s);
+    if (st) return st;
     int passes = 1;
     int64_t n_tail = (int64_t)hh.tail[0];
     if (want_var && !(n_tail < T && T <= n_tail + (int64_t)hh.cand_count && hh.cand_count <= kNoAllocCandidates)) {
@@ -263,6 +267,8 @@ extern "C" int rg_simulate_noalloc(const rg_portfolio *h, const rg_query *q, rg_
         NA_TRY(query_launch(p, q, a, sms, s));
         NA_TRY(cudaMemcpyAsync(hist, dhist, sizeof(hist), cudaMemcpyDeviceToHost, s));
         NA_TRY(cudaStreamSynchronize(s));
+        st = query_pass_status(p, q, s);
+        if (st) return st;
         int64_t cum = 0;
         int j = 0;
         for (; j < kVarHistBins + 2; j++) {
@@ -281,6 +287,8 @@ extern "C" int rg_simulate_noalloc(const rg_portfolio *h, const rg_query *q, rg_
         NA_TRY(cudaMemcpyAsync(&hh.tail, dh->tail, sizeof(hh.tail), cudaMemcpyDeviceToHost, s));
         NA_TRY(cudaMemcpyAsync(&hh.cand_count, &dh->cand_count, sizeof(hh.cand_count), cudaMemcpyDeviceToHost, s));
         NA_TRY(cudaStreamSynchronize(s));
+        st = query_pass_status(p, q, s);
+        if (st) return st;
         n_tail = (int64_t)hh.tail[0];
         passes = 3;
         if (n_tail != cum || hh.cand_count != hist[j])

@@ -33,6 +33,21 @@
  *                        hi), block = day*ceil(N/4) + asset/4; Box-Muller
  *                        (Box & Muller 1958) on each pair of words; H daily
  *                        draws summed per asset; R = H*mu + L*sum(Z).
+ *   orc_factor_crash_prob
+ *                        FP64 P(S >= k) for a factor covariance
+ *                        Sigma = B B^T + diag(idio^2) and an H-day horizon
+ *                        with summed daily draws: R = H mu + sqrt(H)(B F +
+ *                        idio e) in distribution, F ~ N(0, I_nf), e ~ N(0, I_n).
+ *                        Given F the crashes are independent with
+ *                        p_i(F) = Phi((-x - H mu_i - sqrt(H) B_i.F)/(sqrt(H) idio_i)),
+ *                        and P(S >= k | F) is the upper tail of a
+ *                        Poisson-binomial law (recursion over the assets on
+ *                        the counts 0..k-1 with ">= k" absorbing).  The
+ *                        caller supplies the factor points F (randomised
+ *                        quasi-Monte Carlo) and averages over randomisations.
+ *                        No counterpart in the reference (its estimator is
+ *                        plain Monte Carlo); it is the FP64 answer that the
+ *                        sampled estimates are compared with.
  * Compile with -ffp-contract=off so results do not depend on whether the
  * host compiler fuses multiply-adds (explicit fma() is used where the GPU
  * form being mirrored fuses).
@@ -311,4 +326,58 @@ void orc_mc_philox(int n, const double *mu, const double *L, const double *w, in
     }
     counts[0] = crash;
     counts[1] = breach;
+}
+
+
+/* Mean over the npts factor points F (npts x nf, row-major) of
+ * P(S >= k | F), see the header.  Points are split in fixed contiguous
+ * ranges per thread and the partial sums added in thread order, so the
+ * result does not depend on scheduling. */
+double orc_factor_crash_prob(int n, int nf, int horizon, const double *mu, const double *B,
+                             const double *idio, double x, int k, long long npts, const double *F,
+                             int nthreads)
+{
+    if (n < 1 || nf < 1 || k < 1 || npts < 1) return NAN;
+    if (k > n) return 0.0;
+    const double H = (double)horizon, sh = sqrt(H);
+    int nt = 1;
+#ifdef _OPENMP
+    nt = nthreads > 0 ? nthreads : omp_get_max_threads();
+#else
+    (void)nthreads;
+#endif
+    double *part = (double *)calloc((size_t)nt, sizeof(double));
+    if (!part) return NAN;
+#pragma omp parallel num_threads(nt)
+    {
+        int t = 0;
+#ifdef _OPENMP
+        t = omp_get_thread_num();
+#endif
+        const long long lo = npts * t / nt, hi = npts * (t + 1) / nt;
+        double *d = (double *)malloc(sizeof(double) * (size_t)(k + 1));
+        double acc = 0.0;
+        for (long long q = lo; q < hi && d; q++) {
+            const double *f = F + q * nf;
+            for (int j = 0; j <= k; j++) d[j] = 0.0;
+            d[0] = 1.0;
+            for (int i = 0; i < n; i++) {
+                double bf = 0.0;
+                for (int c = 0; c < nf; c++) bf += B[(size_t)i * nf + c] * f[c];
+                const double z = (-x - H * mu[i] - sh * bf) / (sh * idio[i]);
+                const double p = 0.5 * erfc(-z / sqrt(2.0));
+                const double r = 1.0 - p;
+                d[k] += d[k - 1] * p;
+                for (int j = k - 1; j >= 1; j--) d[j] = d[j] * r + d[j - 1] * p;
+                d[0] *= r;
+            }
+            acc += d[k];
+        }
+        free(d);
+        part[t] = acc;
+    }
+    double sum = 0.0;
+    for (int t = 0; t < nt; t++) sum += part[t];
+    free(part);
+    return sum / (double)npts;
 }

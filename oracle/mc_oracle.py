@@ -37,6 +37,7 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(HERE, "_build", "liboracle.so")
 REF_LIB_PATH = os.path.join(HERE, "_ref", "libref_cpu.so")
 CURAND_LIB_PATH = os.path.join(HERE, "_build", "liborc_curand.so")
+REF_KERNEL_PATH = os.path.join(HERE, "_ref", "ref_kernel.fatbin")
 
 _lib = None
 _ref = None
@@ -88,6 +89,10 @@ def lib():
         L.orc_cholesky_lower.argtypes = [ctypes.c_int, _dp, ctypes.c_longlong, _dp]
         L.orc_cholesky_lower.restype = ctypes.c_int
         L.orc_stats.argtypes = [ctypes.c_longlong, ctypes.c_longlong, ctypes.POINTER(OrcResult)]
+        L.orc_factor_crash_prob.argtypes = [ctypes.c_int, ctypes.c_int, ctypes.c_int, _dp, _dp, _dp,
+                                            ctypes.c_double, ctypes.c_int, ctypes.c_longlong, _dp,
+                                            ctypes.c_int]
+        L.orc_factor_crash_prob.restype = ctypes.c_double
         _lib = L
     return _lib
 
@@ -120,6 +125,10 @@ def curand_lib():
                                          ctypes.c_int, _dp]
         C.orc_curand_philox_words.argtypes = [ctypes.c_ulonglong, ctypes.c_ulonglong,
                                               ctypes.c_longlong, ctypes.c_int, _u32p]
+        C.orc_ref_kernel_load.argtypes = [ctypes.c_char_p]
+        C.orc_ref_kernel_run.argtypes = [ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_double,
+                                         ctypes.c_void_p, ctypes.c_void_p, ctypes.c_ulong, ctypes.c_void_p,
+                                         ctypes.c_void_p, ctypes.c_void_p, ctypes.POINTER(ctypes.c_float)]
         _curand = C
     return _curand
 
@@ -136,6 +145,27 @@ def curand_philox_words(seed, M, blocks, path0=0):
     if curand_lib().orc_curand_philox_words(seed, path0, M, blocks, out.ctypes.data_as(_u32p)) != 0:
         raise RuntimeError("cuRAND Philox helper failed")
     return out
+
+
+def ref_kernel_available() -> bool:
+    """True where the reference's own GPU kernel has been compiled (make
+    refcuda, which needs the reference tree)."""
+    return os.path.exists(REF_KERNEL_PATH)
+
+
+def ref_kernel_run(M, N, k, x, d_mu, d_L, seed, d_S, d_count, stream=None):
+    """One launch of the reference's monte_carlo_kernel
+    (src/05-GPU/monte_carlos_cuda.cu:23-72) as its host wrapper launches it
+    (.cu:121-128), on device buffers given as integer addresses; returns the
+    launch's device time in ms."""
+    C = curand_lib()
+    if C.orc_ref_kernel_load(REF_KERNEL_PATH.encode()) != 0:
+        raise RuntimeError("cannot load the reference kernel from " + REF_KERNEL_PATH)
+    ms = ctypes.c_float()
+    if C.orc_ref_kernel_run(int(M), int(N), int(k), float(x), d_mu, d_L, int(seed), d_S, d_count, stream,
+                            ctypes.byref(ms)) != 0:
+        raise RuntimeError("reference kernel launch failed")
+    return ms.value
 
 
 def _d(a):
@@ -313,6 +343,31 @@ def one_factor_crash_prob(mu, beta, market_vol, idio, x, k, horizon=1, nodes=96)
             dist[0] *= (1 - pi)
         total += a * dist[k:].sum()
     return float(total)
+
+
+def factor_crash_prob(mu, B, idio, x, k, horizon=1, log2_points=20, scrambles=8, nthreads=0, seed=0):
+    """FP64 P(S >= k) for Sigma = B B^T + diag(idio^2) (B is N x F) over an
+    H-day horizon with summed daily draws (mc_oracle.c:
+    orc_factor_crash_prob): the factor-conditional Poisson-binomial tail
+    averaged over F ~ N(0, I_F) by randomised quasi-Monte Carlo -- `scrambles`
+    independently scrambled Sobol' sets of 2^log2_points points each, mapped
+    to normals by the inverse CDF.  Returns (estimate, standard error), the
+    error from the spread of the independent scrambles."""
+    from scipy.stats import norm, qmc
+    mu = np.ascontiguousarray(mu, dtype=np.float64)
+    B = np.ascontiguousarray(np.atleast_2d(np.asarray(B, dtype=np.float64).T).T)
+    idio = np.ascontiguousarray(idio, dtype=np.float64)
+    n, nf = B.shape
+    (mu, pmu), (B, pB), (idio, pid) = _d(mu), _d(B), _d(idio)
+    est = []
+    for r in range(scrambles):
+        U = qmc.Sobol(nf, scramble=True, seed=seed + r).random_base2(log2_points)
+        F, pF = _d(norm.ppf(U))
+        est.append(lib().orc_factor_crash_prob(n, nf, int(horizon), pmu, pB, pid, float(x),
+                                                int(k), F.shape[0], pF, int(nthreads)))
+    est = np.array(est)
+    se = float(est.std(ddof=1) / math.sqrt(len(est))) if len(est) > 1 else float("nan")
+    return float(est.mean()), se
 
 
 # ---------------------------------------------------- empirical tail

@@ -21,8 +21,9 @@ def test_reference_arm_line():
         assert key in d, key
     assert d["impl"] == "reference" and d["metric"] == "paths_per_second" and d["unit"] == "paths/s"
     assert d["value"] > 0 and d["higher_is_better"] is True
-    assert d["config"]["workload"] == "one_factor_50"
+    assert d["config"]["workload"] == "five_factor_600" and d["config"]["n_assets"] == 600
     assert d["cpu_baseline"]["kind"] in ("reference", "port") and d["cpu_baseline"]["cores"] >= 1
     assert d["e2e"]["h2d_bytes_per_step"] == 0 and d["e2e"]["d2h_bytes_per_step"] == 0
     assert d["e2e"]["value"] == d["value"]
-    assert d["sample_paths_per_step"] > 0 and d["ms_per_step_basis"].startswith("extrapolated")
+    assert d["sample_paths_per_step"] > 0 and d["ms_per_step_basis"].startswith("measured")
+    assert d["ms_per_full_step_extrapolated"] > 0

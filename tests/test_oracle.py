@@ -1,6 +1,7 @@
 """Oracle pins (CPU): known-answer vectors, golden vectors from the
 reference's own code, closed forms.  The oracle is only trusted for the GPU
 parity tests because these pass."""
+import math
 import os
 
 import numpy as np
@@ -166,3 +167,44 @@ def test_tail_count_definition(oracle):
     assert oracle.tail_count(100, 0.99) == 1
     assert oracle.tail_count(150, 0.99) == 2
     assert oracle.tail_count(1, 0.99) == 1
+
+
+def test_factor_crash_prob_matches_one_factor_quadrature(oracle):
+    """The multi-factor P(S >= k) oracle (factor-conditional Poisson-binomial
+    tail, randomised QMC) agrees with the one-factor Gauss-Hermite closed form
+    within 4 of its own standard errors, for one and ten days."""
+    from riskgpu import synth
+    rng = np.random.default_rng(67)
+    mu, sigma, beta, idio = synth.one_factor_sigma(rng, 50)
+    for horizon, x, k in ((1, 0.03, 5), (10, 0.08, 8)):
+        gh = oracle.one_factor_crash_prob(mu, beta, 0.012, idio, x, k, horizon)
+        est, se = oracle.factor_crash_prob(mu, 0.012 * beta, idio, x, k, horizon, log2_points=12, scrambles=8)
+        assert se > 0 and abs(est - gh) <= 4 * se + 1e-12, (est, se, gh)
+
+
+def test_oracle_figures_fixture_belongs_to_the_workloads(oracle):
+    """tests/golden/oracle_figures.json (make_oracle_figures.py) was made from
+    the benchmark's synthetic inputs: its checksum matches, its closed forms
+    are recomputed, and its five-factor P(S >= k) agrees with a small fresh
+    oracle run within 4 standard errors."""
+    import hashlib
+    import json
+    from riskgpu import synth
+    figs = json.load(open(os.path.join(GOLDEN, "oracle_figures.json")))
+    for name, make in (("one_factor_50", synth.one_factor_50), ("five_factor_600", synth.five_factor_600)):
+        p = make(n_paths=1)
+        fig = figs[name]
+        h = hashlib.sha256()
+        for a in (p.mu, p.sigma, p.weights):
+            h.update(np.ascontiguousarray(a, dtype=np.float64).tobytes())
+        assert h.hexdigest() == fig["inputs_sha256"], name
+        cf = oracle.portfolio_closed_form(p.mu, p.sigma, p.weights, p.horizon, p.port_threshold, figs["alpha"])
+        for key in ("p_breach", "var", "cvar", "mean", "sd"):
+            assert abs(cf[key] - fig[key]) <= 1e-12 * max(1.0, abs(cf[key])), (name, key)
+        assert (fig["x"], fig["k"], fig["horizon"]) == (p.x, p.k, p.horizon)
+    p = synth.five_factor_600(n_paths=1)
+    rng = np.random.default_rng(600)
+    mu, sigma, B, idio = synth.factor_sigma(rng, p.n, 5, 0.5 * 0.01)
+    est, se = oracle.factor_crash_prob(mu, B, idio, p.x, p.k, p.horizon, log2_points=11, scrambles=4)
+    fig = figs["five_factor_600"]
+    assert abs(est - fig["p_crash"]) <= 4 * math.hypot(se, fig["p_crash_se"]), (est, se, fig["p_crash"])

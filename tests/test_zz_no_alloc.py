@@ -8,6 +8,9 @@ statistic, CVaR within 1e-9 relative (the two sum the tail in different
 orders), on two calls in a row (the second call finds the previous call's
 data in the shared scratch array and must clear what it relies on).
 
+The tensor-core forms (FP16x3, BF16x3) go through the same entry point and
+report a bounded wait that ran out as RG_ERR_TIMEOUT, like rg_simulate.
+
 Collected last (file name) so that a failure here comes after every other
 test has run; it also passes alone in a fresh process.
 """
@@ -78,3 +81,50 @@ def test_noalloc_rejects_oversized_queries(gpu):
     st, _ = _noalloc(gpu, port, q)
     assert st == gpu.RG_ERR_UNSUPPORTED
     assert b"scratch array" in gpu.lib().rg_last_error()
+
+
+def _factor_case(gpu, n, seed):
+    from riskgpu import synth
+    rng = np.random.default_rng(seed)
+    mu, sigma, _, _ = synth.factor_sigma(rng, n, 5, 0.5 * 0.01)
+    w = rng.dirichlet(np.ones(n))
+    return gpu.Portfolio(mu, sigma, w)
+
+
+@pytest.mark.parametrize("var_level", [0.99, 0.0])
+@pytest.mark.parametrize("prec", ["fp16x3", "bf16x3"])
+def test_noalloc_tensor_forms_match_rg_simulate(gpu, prec, var_level):
+    """The tcgen05 kernels through the allocation-free entry point give the
+    same counts and VaR order statistic as through rg_simulate, on two
+    calls in a row."""
+    code = {"fp16x3": gpu.PREC_FP16X3, "bf16x3": gpu.PREC_BF16X3}[prec]
+    port = _factor_case(gpu, 300, 29)
+    queries = [gpu.make_query(300_000, 3, x=0.05, k=30, horizon=5, port_threshold=-0.04,
+                              precision=code, var_level=var_level),
+               gpu.make_query(120_001, 4, x=0.03, k=20, horizon=2, port_threshold=-0.03,
+                              precision=code, var_level=var_level)]
+    for q in queries:
+        ref = port.simulate(q)
+        st, got = _noalloc(gpu, port, q)
+        assert st == gpu.RG_OK, gpu.lib().rg_last_error()
+        _same(got, ref)
+
+
+@pytest.mark.parametrize("var_level", [0.99, 0.0])
+def test_noalloc_tensor_bounded_wait_reports_timeout(gpu, monkeypatch, var_level):
+    """Failure detection without a GPU fault: RG_FAULT_INJECT=tcstall leaves
+    one pipeline stage of the tensor-core kernel unfilled, its bounded wait
+    runs out and it sets its error word; the allocation-free entry point
+    returns RG_ERR_TIMEOUT instead of incomplete counts, and the next call
+    on the same context succeeds."""
+    port = _factor_case(gpu, 200, 3)
+    q = gpu.make_query(65_536, 1, x=0.02, k=5, port_threshold=-0.03, precision=gpu.PREC_BF16X3,
+                       var_level=var_level)
+    monkeypatch.setenv("RG_FAULT_INJECT", "tcstall")
+    st, _ = _noalloc(gpu, port, q)
+    assert st == gpu.RG_ERR_TIMEOUT, gpu.lib().rg_last_error()
+    assert b"bounded wait" in gpu.lib().rg_last_error()
+    monkeypatch.delenv("RG_FAULT_INJECT")
+    st, got = _noalloc(gpu, port, q)
+    assert st == gpu.RG_OK, gpu.lib().rg_last_error()
+    _same(got, port.simulate(q))
