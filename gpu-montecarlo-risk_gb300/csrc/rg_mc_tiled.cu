@@ -1,8 +1,12 @@
-// Plain fused FP32 Monte Carlo kernel for any asset count (the general-N
+// Plain fused FP32 Monte Carlo kernels for any asset count (the general-N
 // counterpart of the N <= 64 kernel; the reference caps N at 64,
-// src/05-GPU/monte_carlos_cuda.cu:34,78-81).
+// src/05-GPU/monte_carlos_cuda.cu:34,78-81).  Three forms, each described
+// at its definition: the two-CTA mc_tiled2_kernel (default), the
+// phase-serial mc_tiled_kernel (RG_PLAIN_KERNEL=serial) and the
+// warp-specialised mc_tiled_ws_kernel (RG_PLAIN_KERNEL=ws).
 //
-// A CTA owns a tile of 64 paths at a time (grid-stride over tiles):
+// Phase-serial form: a CTA owns a tile of 64 paths at a time (grid-stride
+// over tiles):
 //  1. Normals.  The 256 threads draw the tile's normals (Philox4x32-10 in
 //     the engine layout, Box-Muller, summed over the H days -- or one
 //     N(0, H) draw per asset in the aggregated mode) into shared memory,
@@ -20,7 +24,8 @@
 //     flags and the VaR bookkeeping.
 // Shared memory: 4 * 64 * Kpad bytes for Z (155 KB at N = 600) + 8 KB of L
 // staging + 8 KB of partials (+ 16 KB of VaR histogram): one CTA per SM,
-// N <= 768.
+// N <= 768.  Generation and the GEMM take turns on 8 warps per SM.
+#include <cstdlib>
 #include <cstring>
 #include "rg_fused_kernel.cuh"
 
@@ -35,7 +40,7 @@ struct TiledArgs {
     PlainArgs a;          // counters, thresholds, Philox keys, VaR fields
     const float *Lt;      // [kpad][npad] L^T, FP32, zero padded
     int kpad;             // N rounded up to kTK
-    int npad;             // N rounded up to kTN
+    int npad;             // N rounded up to 256 (a multiple of both column-block widths)
     int aggregated;       // 1: one N(0, H) draw per asset (sqrt(H) z)
     float sqrt_h;
 };
@@ -217,6 +222,422 @@ __global__ void __launch_bounds__(kTiledThreads, 1) mc_tiled_kernel(const TiledA
     cta_flush(a, crash, breach, n_tail, tail_fx, sacc, VAR ? shist : nullptr, VAR);
 }
 
+// ---------------------------------------------------------------------------
+// Warp-specialised form (RG_PLAIN_KERNEL=ws): normal generation and the GEMM run
+// at the same time on different warps of one CTA per SM (512 threads).
+//   warps 8-15  generator: draw the normals of a 32-path tile (Philox4x32-10
+//               + Box-Muller, summed over the H days, or one N(0, H) draw per
+//               asset) into one slot of a two-slot ring Zs[slot][k][p];
+//   warps 0-7   GEMM: R = H mu + L Z over 256-asset column blocks, 4-path x
+//               8-asset register tiles accumulated with packed __ffma2_rn,
+//               L^T slices (8 x 256) staged by cp.async, double buffered.
+//               Warp w holds assets c0 + 32w .. c0 + 32w + 31 of a block, so
+//               its K loop stops at c0 + 32(w + 1) (L is lower triangular:
+//               about 8 % of the multiply-adds at N = 600 are padding, 36 %
+//               with a cut per 128-asset block), and a warp whose assets are
+//               all >= N skips the block.
+// Handoff by named barriers: FULL[s] (ids 2, 3) completes when the 256
+// generator threads have arrived after writing slot s and the 256 GEMM
+// threads sync on it; EMPTY[s] (ids 4, 5) completes when the GEMM threads
+// have arrived after their last read of slot s and the generator threads
+// sync on it before refilling it.  Both roles walk the same static tile
+// list, so the arrivals and waits pair up by construction (the GEMM side
+// skips the EMPTY arrival of its last two tiles, which nobody waits for).
+// Per column block the crash counts and w.R partial sums of a warp's 32
+// assets are reduced across its lanes by shuffles, then over the 8 warps in
+// warp order by the path's own thread (deterministic).  Each asset's return
+// is the same FMA chain in k order as in the phase-serial kernel, so S per
+// path is identical between the two.
+// Shared memory: 2 x 128 x Kpad bytes for Z (154 KB at N = 600) + 16 KB of
+// L staging + 2 KB of partials (+ 16 KB of VaR histogram): N <= 768.
+static constexpr int kWsP = 32;
+static constexpr int kWsTN = 256;
+static constexpr int kWsThreadsT = 512;
+static constexpr int kWsHalf = 256;
+
+__device__ __forceinline__ void nbar_sync(int id, int count)
+{
+    asm volatile("bar.sync %0, %1;" ::"r"(id), "r"(count) : "memory");
+}
+__device__ __forceinline__ void nbar_arrive(int id, int count)
+{
+    asm volatile("bar.arrive %0, %1;" ::"r"(id), "r"(count) : "memory");
+}
+
+template <bool VAR>
+__global__ void __launch_bounds__(kWsThreadsT, 1) mc_tiled_ws_kernel(const TiledArgs t)
+{
+    extern __shared__ __align__(16) float smem[];
+    const PlainArgs &a = t.a;
+    const int kpad = t.kpad;
+    float *Zs = smem;                                  // [2][kpad][kWsP]
+    float *Ls = Zs + 2 * (size_t)kpad * kWsP;          // [2][kTK][kWsTN]
+    int *partS = (int *)(Ls + 2 * kTK * kWsTN);        // [8][kWsP]
+    float *partP = (float *)(partS + 8 * kWsP);        // [8][kWsP]
+    __shared__ unsigned long long sacc[4];
+    __shared__ unsigned int shist[VAR ? kVarHistBins + 2 : 1];
+
+    const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+    if (tid < 4) sacc[tid] = 0ull;
+    if (VAR && a.var_mode == 2)
+        for (int i = tid; i < a.sel_bins + 2; i += blockDim.x) shist[i] = 0u;
+    __syncthreads();
+    int crash = 0, breach = 0, n_tail = 0;
+    long long tail_fx = 0;
+    const int n = a.n;
+    const int nq = (n + 3) >> 2;
+    const long long ntiles = (a.n_paths + kWsP - 1) / kWsP;
+    const long long my_tiles = (long long)blockIdx.x < ntiles ? (ntiles - 1 - blockIdx.x) / gridDim.x + 1 : 0;
+
+    if (warp >= 8) {
+        // ============================ generator ============================
+        const int gt = tid - kWsHalf;
+        const int days = t.aggregated ? 1 : a.horizon;
+        const int items = kWsP * (kpad / 4);
+        for (long long j = 0; j < my_tiles; j++) {
+            const int s = (int)(j & 1);
+            if (j >= 2) nbar_sync(4 + s, kWsThreadsT); // slot s released by the GEMM warps
+            const long long p0 = ((long long)blockIdx.x + j * gridDim.x) * kWsP;
+            float *Z = Zs + (size_t)s * kpad * kWsP;
+            for (int it = gt; it < items; it += kWsHalf) {
+                const int p = it & (kWsP - 1), q = it >> 5;
+                float4 z = make_float4(0.f, 0.f, 0.f, 0.f);
+                if (q < nq) {
+                    const unsigned long long path = a.path0 + (unsigned long long)(p0 + p);
+                    const uint32_t plo = (uint32_t)path, phi = (uint32_t)(path >> 32);
+                    for (int d = 0; d < days; d++) {
+                        const uint4 wv = rg_philox(make_uint4((uint32_t)(d * nq + q), 0u, plo, phi), a.keys);
+                        float z0, z1, z2, z3;
+                        rg_box_muller(wv.x, wv.y, z0, z1);
+                        rg_box_muller(wv.z, wv.w, z2, z3);
+                        z.x += z0;
+                        z.y += z1;
+                        z.z += z2;
+                        z.w += z3;
+                    }
+                    if (t.aggregated) {
+                        z.x *= t.sqrt_h;
+                        z.y *= t.sqrt_h;
+                        z.z *= t.sqrt_h;
+                        z.w *= t.sqrt_h;
+                    }
+                }
+                Z[(4 * q + 0) * kWsP + p] = z.x;
+                Z[(4 * q + 1) * kWsP + p] = z.y;
+                Z[(4 * q + 2) * kWsP + p] = z.z;
+                Z[(4 * q + 3) * kWsP + p] = z.w;
+            }
+            __threadfence_block();
+            nbar_arrive(2 + s, kWsThreadsT); // slot s full
+        }
+    } else {
+        // ============================== GEMM ===============================
+        const int pg = tid & 7, ag = tid >> 3; // paths 4pg..4pg+3; assets 8ag..8ag+7 of a block
+        const int ncb = (n + kWsTN - 1) / kWsTN;
+        for (long long j = 0; j < my_tiles; j++) {
+            const int s = (int)(j & 1);
+            nbar_sync(2 + s, kWsThreadsT); // slot s full
+            const long long p0 = ((long long)blockIdx.x + j * gridDim.x) * kWsP;
+            const float *Z = Zs + (size_t)s * kpad * kWsP;
+            int totS = 0;      // threads 0..31: path p0 + tid
+            float totP = 0.f;
+            for (int cb = 0; cb < ncb; cb++) {
+                const int c0 = cb * kWsTN;
+                const int kmax = min(kpad, c0 + kWsTN);
+                const int wlo = c0 + 32 * warp;
+                const int kend = min(kpad, wlo + 32);
+                const bool active = wlo < n;
+                float2 acc[4][4];
+#pragma unroll
+                for (int i = 0; i < 4; i++)
+#pragma unroll
+                    for (int jj = 0; jj < 4; jj++) acc[i][jj] = make_float2(0.f, 0.f);
+                const int sk = tid >> 5, sc = tid & 31; // staging: row sk, columns 8sc..8sc+7
+                cp_async16(&Ls[sk * kWsTN + 8 * sc], &t.Lt[(size_t)sk * t.npad + c0 + 8 * sc]);
+                cp_async16(&Ls[sk * kWsTN + 8 * sc + 4], &t.Lt[(size_t)sk * t.npad + c0 + 8 * sc + 4]);
+                cp_async_commit();
+                int buf = 0;
+                for (int k0 = 0; k0 < kmax; k0 += kTK) {
+                    cp_async_wait_all();
+                    nbar_sync(1, kWsHalf);
+                    if (k0 + kTK < kmax) {
+                        float *dst = Ls + (buf ^ 1) * kTK * kWsTN + sk * kWsTN + 8 * sc;
+                        const float *src = &t.Lt[(size_t)(k0 + kTK + sk) * t.npad + c0 + 8 * sc];
+                        cp_async16(dst, src);
+                        cp_async16(dst + 4, src + 4);
+                        cp_async_commit();
+                    }
+                    if (active && k0 < kend) {
+                        const float *Lb = Ls + buf * kTK * kWsTN;
+#pragma unroll
+                        for (int kk = 0; kk < kTK; kk++) {
+                            const float4 z = *reinterpret_cast<const float4 *>(&Z[(k0 + kk) * kWsP + 4 * pg]);
+                            const float4 l0 = *reinterpret_cast<const float4 *>(&Lb[kk * kWsTN + 8 * ag]);
+                            const float4 l1 = *reinterpret_cast<const float4 *>(&Lb[kk * kWsTN + 8 * ag + 4]);
+                            const float zz[4] = {z.x, z.y, z.z, z.w};
+#pragma unroll
+                            for (int i = 0; i < 4; i++) {
+                                const float2 zi = make_float2(zz[i], zz[i]);
+                                acc[i][0] = __ffma2_rn(make_float2(l0.x, l0.y), zi, acc[i][0]);
+                                acc[i][1] = __ffma2_rn(make_float2(l0.z, l0.w), zi, acc[i][1]);
+                                acc[i][2] = __ffma2_rn(make_float2(l1.x, l1.y), zi, acc[i][2]);
+                                acc[i][3] = __ffma2_rn(make_float2(l1.z, l1.w), zi, acc[i][3]);
+                            }
+                        }
+                    }
+                    buf ^= 1;
+                }
+                // block epilogue: this thread's 4 paths x 8 assets, then the
+                // warp's 4 asset groups (lanes pg, pg+8, pg+16, pg+24)
+                float hm[8], wt[8];
+#pragma unroll
+                for (int jj = 0; jj < 8; jj++) {
+                    const int c = c0 + 8 * ag + jj;
+                    hm[jj] = (c < n) ? (float)((double)a.horizon * a.mu64[c]) : 0.f;
+                    wt[jj] = (c < n) ? a.w[c] : 0.f;
+                }
+#pragma unroll
+                for (int i = 0; i < 4; i++) {
+                    int sv = 0;
+                    float pw = 0.f;
+#pragma unroll
+                    for (int jj = 0; jj < 4; jj++) {
+                        const int a0 = c0 + 8 * ag + 2 * jj;
+                        const float r0 = hm[2 * jj] + acc[i][jj].x;
+                        const float r1 = hm[2 * jj + 1] + acc[i][jj].y;
+                        sv += (a0 < n && r0 < a.neg_x) ? 1 : 0;
+                        sv += (a0 + 1 < n && r1 < a.neg_x) ? 1 : 0;
+                        pw = fmaf(wt[2 * jj], r0, pw);
+                        pw = fmaf(wt[2 * jj + 1], r1, pw);
+                    }
+                    sv += __shfl_xor_sync(0xffffffffu, sv, 8);
+                    pw += __shfl_xor_sync(0xffffffffu, pw, 8);
+                    sv += __shfl_xor_sync(0xffffffffu, sv, 16);
+                    pw += __shfl_xor_sync(0xffffffffu, pw, 16);
+                    if (lane < 8) {
+                        partS[warp * kWsP + 4 * pg + i] = sv;
+                        partP[warp * kWsP + 4 * pg + i] = pw;
+                    }
+                }
+                nbar_sync(1, kWsHalf);
+                if (tid < kWsP) {
+#pragma unroll
+                    for (int w = 0; w < 8; w++) {
+                        totS += partS[w * kWsP + tid];
+                        totP += partP[w * kWsP + tid];
+                    }
+                }
+                // partS / partP are rewritten only after the next block's
+                // first barrier; Ls only after this one
+            }
+            // every read of slot s is done: the generator may refill it
+            if (j + 2 < my_tiles) nbar_arrive(4 + s, kWsThreadsT);
+            if (tid < kWsP) {
+                const long long p = p0 + tid;
+                if (p < a.n_paths) {
+                    crash += (totS >= a.k) ? 1 : 0;
+                    breach += (a.has_w && totP < a.port_thr) ? 1 : 0;
+                    if (a.s_values) a.s_values[p] = totS;
+                    if (a.port_values) a.port_values[p] = totP;
+                    if (VAR) var_path(a, totP, shist, n_tail, tail_fx);
+                }
+            }
+        }
+    }
+    cta_flush(a, crash, breach, n_tail, tail_fx, sacc, VAR ? shist : nullptr, VAR);
+}
+
+// ---------------------------------------------------------------------------
+// Two-CTA form (the default): the phase-serial scheme on 32-path tiles with
+// 512 threads a CTA and two CTAs per SM, so that one CTA's normal
+// generation overlaps the other's GEMM (32 warps per SM, each CTA taking
+// its turns independently).
+//   1. normals: item (path p, quad q) -> Zs[4q .. 4q+3][p], 32 paths a row;
+//   2. GEMM over 256-asset column blocks: 4-path x 4-asset register tiles
+//      (packed __ffma2_rn), L^T slices (8 x 256) staged by cp.async, double
+//      buffered; warp w holds assets c0 + 16w .. c0 + 16w + 15 and stops its
+//      K loop at c0 + 16(w + 1) (lower triangle, about 4 % padding at N = 600);
+//      a warp whose assets are all >= N skips the block;
+//   3. per block, a thread's 4 x 4 returns -> crash counts and w.R partial
+//      sums, reduced over the warp's 4 asset groups by shuffles, then over
+//      the 16 warps in warp order by the path's own thread (deterministic).
+// Each asset's return is the same FMA chain in k order as in the other two
+// forms, so S per path is identical between them.  64 registers a thread.
+// Shared memory: 128 x Kpad bytes for Z (77 KB at N = 600) + 16 KB of L
+// staging + 4 KB of partials (+ 16 KB of VaR histogram); two CTAs per SM up
+// to N = 600 without the histogram, one CTA above (the launcher asks the
+// occupancy calculator).
+static constexpr int kDuP = 32;
+static constexpr int kDuTN = 256;
+static constexpr int kDuThreads = 512;
+static constexpr int kDuWarps = kDuThreads / 32;
+
+template <bool VAR>
+__global__ void __launch_bounds__(kDuThreads, 2) mc_tiled2_kernel(const TiledArgs t)
+{
+    extern __shared__ __align__(16) float smem[];
+    const PlainArgs &a = t.a;
+    const int kpad = t.kpad;
+    float *Zs = smem;                                  // [kpad][kDuP]
+    float *Ls = Zs + (size_t)kpad * kDuP;              // [2][kTK][kDuTN]
+    int *partS = (int *)(Ls + 2 * kTK * kDuTN);        // [kDuWarps][kDuP]
+    float *partP = (float *)(partS + kDuWarps * kDuP); // [kDuWarps][kDuP]
+    __shared__ unsigned long long sacc[4];
+    __shared__ unsigned int shist[VAR ? kVarHistBins + 2 : 1];
+
+    const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+    if (tid < 4) sacc[tid] = 0ull;
+    if (VAR && a.var_mode == 2)
+        for (int i = tid; i < a.sel_bins + 2; i += blockDim.x) shist[i] = 0u;
+    int crash = 0, breach = 0, n_tail = 0;
+    long long tail_fx = 0;
+    const int n = a.n;
+    const int nq = (n + 3) >> 2;
+    const int ncb = (n + kDuTN - 1) / kDuTN;
+    const int days = t.aggregated ? 1 : a.horizon;
+    const int items = kDuP * (kpad / 4);
+    const int pg = tid & 7, ag = tid >> 3;     // paths 4pg..4pg+3; assets 4ag..4ag+3 of a block
+    const int sk = tid >> 6, sc = tid & 63;    // staging: row sk, columns 4sc..4sc+3
+    const long long ntiles = (a.n_paths + kDuP - 1) / kDuP;
+
+    for (long long tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
+        const long long p0 = tile * kDuP;
+        // ---- 1. normals into Zs[k][p]
+        for (int it = tid; it < items; it += kDuThreads) {
+            const int p = it & (kDuP - 1), q = it >> 5;
+            float4 z = make_float4(0.f, 0.f, 0.f, 0.f);
+            if (q < nq) {
+                const unsigned long long path = a.path0 + (unsigned long long)(p0 + p);
+                const uint32_t plo = (uint32_t)path, phi = (uint32_t)(path >> 32);
+                for (int d = 0; d < days; d++) {
+                    const uint4 wv = rg_philox(make_uint4((uint32_t)(d * nq + q), 0u, plo, phi), a.keys);
+                    float z0, z1, z2, z3;
+                    rg_box_muller(wv.x, wv.y, z0, z1);
+                    rg_box_muller(wv.z, wv.w, z2, z3);
+                    z.x += z0;
+                    z.y += z1;
+                    z.z += z2;
+                    z.w += z3;
+                }
+                if (t.aggregated) {
+                    z.x *= t.sqrt_h;
+                    z.y *= t.sqrt_h;
+                    z.z *= t.sqrt_h;
+                    z.w *= t.sqrt_h;
+                }
+            }
+            Zs[(4 * q + 0) * kDuP + p] = z.x;
+            Zs[(4 * q + 1) * kDuP + p] = z.y;
+            Zs[(4 * q + 2) * kDuP + p] = z.z;
+            Zs[(4 * q + 3) * kDuP + p] = z.w;
+        }
+        __syncthreads();
+
+        // ---- 2./3. column blocks
+        int totS = 0;      // threads 0..31: path p0 + tid
+        float totP = 0.f;
+        for (int cb = 0; cb < ncb; cb++) {
+            const int c0 = cb * kDuTN;
+            const int kmax = min(kpad, c0 + kDuTN);
+            const int wlo = c0 + 16 * warp;
+            const int kend = min(kpad, wlo + 16);
+            const bool active = wlo < n;
+            float2 acc[4][2];
+#pragma unroll
+            for (int i = 0; i < 4; i++) {
+                acc[i][0] = make_float2(0.f, 0.f);
+                acc[i][1] = make_float2(0.f, 0.f);
+            }
+            cp_async16(&Ls[sk * kDuTN + 4 * sc], &t.Lt[(size_t)sk * t.npad + c0 + 4 * sc]);
+            cp_async_commit();
+            int buf = 0;
+            for (int k0 = 0; k0 < kmax; k0 += kTK) {
+                cp_async_wait_all();
+                __syncthreads();
+                if (k0 + kTK < kmax) {
+                    cp_async16(&Ls[(buf ^ 1) * kTK * kDuTN + sk * kDuTN + 4 * sc],
+                               &t.Lt[(size_t)(k0 + kTK + sk) * t.npad + c0 + 4 * sc]);
+                    cp_async_commit();
+                }
+                if (active && k0 < kend) {
+                    const float *Lb = Ls + buf * kTK * kDuTN;
+#pragma unroll
+                    for (int kk = 0; kk < kTK; kk++) {
+                        const float4 z = *reinterpret_cast<const float4 *>(&Zs[(k0 + kk) * kDuP + 4 * pg]);
+                        const float4 l = *reinterpret_cast<const float4 *>(&Lb[kk * kDuTN + 4 * ag]);
+                        const float zz[4] = {z.x, z.y, z.z, z.w};
+#pragma unroll
+                        for (int i = 0; i < 4; i++) {
+                            const float2 zi = make_float2(zz[i], zz[i]);
+                            acc[i][0] = __ffma2_rn(make_float2(l.x, l.y), zi, acc[i][0]);
+                            acc[i][1] = __ffma2_rn(make_float2(l.z, l.w), zi, acc[i][1]);
+                        }
+                    }
+                }
+                buf ^= 1;
+            }
+            float hm[4], wt[4];
+#pragma unroll
+            for (int jj = 0; jj < 4; jj++) {
+                const int c = c0 + 4 * ag + jj;
+                hm[jj] = (c < n) ? (float)((double)a.horizon * a.mu64[c]) : 0.f;
+                wt[jj] = (c < n) ? a.w[c] : 0.f;
+            }
+#pragma unroll
+            for (int i = 0; i < 4; i++) {
+                int sv = 0;
+                float pw = 0.f;
+#pragma unroll
+                for (int jj = 0; jj < 2; jj++) {
+                    const int a0 = c0 + 4 * ag + 2 * jj;
+                    const float r0 = hm[2 * jj] + acc[i][jj].x;
+                    const float r1 = hm[2 * jj + 1] + acc[i][jj].y;
+                    sv += (a0 < n && r0 < a.neg_x) ? 1 : 0;
+                    sv += (a0 + 1 < n && r1 < a.neg_x) ? 1 : 0;
+                    pw = fmaf(wt[2 * jj], r0, pw);
+                    pw = fmaf(wt[2 * jj + 1], r1, pw);
+                }
+                sv += __shfl_xor_sync(0xffffffffu, sv, 8);
+                pw += __shfl_xor_sync(0xffffffffu, pw, 8);
+                sv += __shfl_xor_sync(0xffffffffu, sv, 16);
+                pw += __shfl_xor_sync(0xffffffffu, pw, 16);
+                if (lane < 8) {
+                    partS[warp * kDuP + 4 * pg + i] = sv;
+                    partP[warp * kDuP + 4 * pg + i] = pw;
+                }
+            }
+            __syncthreads();
+            if (tid < kDuP) {
+#pragma unroll
+                for (int w = 0; w < kDuWarps; w++) {
+                    totS += partS[w * kDuP + tid];
+                    totP += partP[w * kDuP + tid];
+                }
+            }
+            // partS / partP are rewritten only after the next block's first
+            // barrier; Ls only after this one
+        }
+        if (tid < kDuP) {
+            const long long p = p0 + tid;
+            if (p < a.n_paths) {
+                crash += (totS >= a.k) ? 1 : 0;
+                breach += (a.has_w && totP < a.port_thr) ? 1 : 0;
+                if (a.s_values) a.s_values[p] = totS;
+                if (a.port_values) a.port_values[p] = totP;
+                if (VAR) var_path(a, totP, shist, n_tail, tail_fx);
+            }
+        }
+        __syncthreads(); // Zs and the partials are rewritten by the next tile
+    }
+    cta_flush(a, crash, breach, n_tail, tail_fx, sacc, VAR ? shist : nullptr, VAR);
+}
+
+size_t tiled2_smem_bytes(int n)
+{
+    const int kpad = (n + kTK - 1) / kTK * kTK;
+    return sizeof(float) * ((size_t)kpad * kDuP + 2 * kTK * kDuTN + 2 * kDuWarps * kDuP);
+}
+
 int tiled_max_n() { return 768; }
 
 size_t tiled_smem_bytes(int n)
@@ -225,9 +646,18 @@ size_t tiled_smem_bytes(int n)
     return sizeof(float) * ((size_t)kpad * kTP + 2 * kTK * kTN + 2 * 16 * kTP);
 }
 
-int tiled_npad(int n) { return (n + kTN - 1) / kTN * kTN; }
+size_t tiled_ws_smem_bytes(int n)
+{
+    const int kpad = (n + kTK - 1) / kTK * kTK;
+    return sizeof(float) * (2 * (size_t)kpad * kWsP + 2 * kTK * kWsTN + 2 * 8 * kWsP);
+}
+
+// npad is a multiple of both column-block widths (128 and 256)
+int tiled_npad(int n) { return (n + kWsTN - 1) / kWsTN * kWsTN; }
 int tiled_kpad(int n) { return (n + kTK - 1) / kTK * kTK; }
 
+// The two-CTA kernel unless RG_PLAIN_KERNEL names "ws" (warp-specialised)
+// or "serial" (phase-serial, 64-path tiles, one CTA per SM).
 cudaError_t launch_tiled(const PlainArgs &a, const float *Lt, bool aggregated, int sm_count,
                          cudaStream_t s)
 {
@@ -240,6 +670,35 @@ cudaError_t launch_tiled(const PlainArgs &a, const float *Lt, bool aggregated, i
     t.npad = tiled_npad(a.n);
     t.aggregated = aggregated ? 1 : 0;
     t.sqrt_h = sqrtf((float)a.horizon);
+    const char *env = getenv("RG_PLAIN_KERNEL");
+    const bool ws = env && strstr(env, "ws") != nullptr;
+    const bool serial = env && strstr(env, "serial") != nullptr;
+    if (!ws && !serial) {
+        const size_t smem = tiled2_smem_bytes(a.n);
+        auto kern = (a.var_mode != 0) ? mc_tiled2_kernel<true> : mc_tiled2_kernel<false>;
+        cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        if (e != cudaSuccess) return e;
+        int per_sm = 0;
+        e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, kDuThreads, smem);
+        if (e != cudaSuccess) return e;
+        if (per_sm < 1) per_sm = 1;
+        long long tiles = (a.n_paths + kDuP - 1) / kDuP;
+        long long grid = (long long)sm_count * per_sm;
+        if (tiles < grid) grid = tiles;
+        kern<<<(unsigned)grid, kDuThreads, smem, s>>>(t);
+        return cudaGetLastError();
+    }
+    if (ws) {
+        const size_t smem = tiled_ws_smem_bytes(a.n);
+        auto kern = (a.var_mode != 0) ? mc_tiled_ws_kernel<true> : mc_tiled_ws_kernel<false>;
+        cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        if (e != cudaSuccess) return e;
+        long long tiles = (a.n_paths + kWsP - 1) / kWsP;
+        long long grid = sm_count;
+        if (tiles < grid) grid = tiles;
+        kern<<<(unsigned)grid, kWsThreadsT, smem, s>>>(t);
+        return cudaGetLastError();
+    }
     const size_t smem = tiled_smem_bytes(a.n);
     auto kern = (a.var_mode != 0) ? mc_tiled_kernel<true> : mc_tiled_kernel<false>;
     cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);

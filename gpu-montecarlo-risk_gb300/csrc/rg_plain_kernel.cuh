@@ -2,7 +2,8 @@
 //
 // Replaces the reference kernel monte_carlo_kernel
 // (src/05-GPU/monte_carlos_cuda.cu:23-72).  One thread owns one path at a
-// time (grid-stride over paths, grid sized to fill every SM):
+// time (grid sized to fill every SM; grid-stride over paths in the Philox
+// layout, a contiguous run of paths per thread in the XORWOW layout):
 //   1. normals in registers: Philox4x32-10 + Box-Muller (engine layout) or
 //      the reference's own cuRAND XORWOW stream (curand_init(seed, path, 0)
 //      + curand_normal_double, rounded to FP32), summed over H days;
@@ -50,8 +51,25 @@ __global__ void __launch_bounds__(kPlainThreads, 2) mc_plain_small_kernel(const 
 
     const int nq = (n + 3) >> 2;
     int crash = 0, breach = 0;
-    const long long stride = (long long)gridDim.x * blockDim.x;
-    for (long long p = (long long)blockIdx.x * blockDim.x + tid; p < a.n_paths; p += stride) {
+    // Philox: grid-stride over paths.  XORWOW: each thread walks a
+    // contiguous run of paths, so the cuRAND state of path p + 1 (the
+    // seeded state advanced by p + 1 subsequences) comes from the saved
+    // state of path p by one cuRAND skipahead_sequence(1) instead of a full
+    // curand_init(seed, p + 1, 0), whose skip-ahead costs about one matrix
+    // product per base-4 digit of the path index.
+    const long long nthreads = (long long)gridDim.x * blockDim.x;
+    const long long gtid = (long long)blockIdx.x * blockDim.x + tid;
+    long long p_begin = gtid, p_end = a.n_paths, p_step = nthreads;
+    if (RNG != RG_RNG_PHILOX) {
+        const long long chunk = (a.n_paths + nthreads - 1) / nthreads;
+        p_begin = gtid * chunk;
+        p_end = p_begin + chunk < a.n_paths ? p_begin + chunk : a.n_paths;
+        p_step = 1;
+    }
+    curandStateXORWOW_t next_state;
+    if (RNG != RG_RNG_PHILOX && p_begin < p_end)
+        curand_init(a.seed, a.path0 + (unsigned long long)p_begin, 0ull, &next_state);
+    for (long long p = p_begin; p < p_end; p += p_step) {
         const unsigned long long path = a.path0 + (unsigned long long)p;
         float z[NP];
 #pragma unroll
@@ -76,8 +94,9 @@ __global__ void __launch_bounds__(kPlainThreads, 2) mc_plain_small_kernel(const 
                 }
             }
         } else {
-            curandStateXORWOW_t st;
-            curand_init(a.seed, path, 0ull, &st);
+            // this path's state as curand_init(seed, path, 0) leaves it
+            curandStateXORWOW_t st = next_state;
+            if (p + 1 < p_end) skipahead_sequence(1ull, &next_state);
             for (int d = 0; d < a.horizon; d++) {
 #pragma unroll
                 for (int j = 0; j < NP; j++)

@@ -13,7 +13,8 @@ Workloads (sizes are the benchmark's):
                   data and path seed 42.
   one_factor_50   N=50,  H=1,  M=1e8, Dirichlet(1) weights, threshold -3%,
                   crash semantics x=0.03, k=5, seed 67 (config.yaml:37).
-  five_factor_600 N=600, H=10 summed daily draws, M=1e7, Dirichlet(1) weights.
+  five_factor_600 N=600, H=10 summed daily draws, M=1e7, Dirichlet(1) weights,
+                  portfolio threshold -0.65%, crash semantics x=10%, k=60.
   batch_256       256 portfolios, N~U{10..600}, H~U{1..20}, M log-uniform
                   [1e4, 1e6], 3-factor covariance with a per-portfolio seed,
                   thresholds U(-5%, -1%).
@@ -87,8 +88,9 @@ def five_factor_600(n_paths: int = 10_000_000) -> Portfolio:
     n = 600
     mu, sigma, _, _ = factor_sigma(rng, n, 5, 0.5 * 0.01)
     w = rng.dirichlet(np.ones(n))
-    # 10-day horizon: per-asset crash at -10%, 60 of 600 assets; portfolio -5%.
-    return Portfolio("five_factor_600", mu, sigma, w, 10, n_paths, 0.10, 60, -0.05, 0.99, 600)
+    # 10-day horizon: per-asset crash at -10%, 60 of 600 assets (P ~ 1%);
+    # portfolio breach below -0.65% (P ~ 1%, about the 99% VaR)
+    return Portfolio("five_factor_600", mu, sigma, w, 10, n_paths, 0.10, 60, -0.0065, 0.99, 600)
 
 
 def batch_256(count: int = 256, base_seed: int = 4096, n_max: int = 600,

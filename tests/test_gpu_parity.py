@@ -426,10 +426,21 @@ def _factor_case(n, seed, factors=5):
     return mu, sigma, w
 
 
-@pytest.mark.parametrize("n,horizon,M", [(65, 1, 20000), (100, 3, 8000), (129, 1, 8000),
-                                         (300, 2, 3000), (600, 10, 1024), (768, 1, 700)])
-def test_tiled_per_path_parity(gpu, oracle, n, horizon, M):
-    """General-N tiled kernel == oracle FP64 restatement per path."""
+# the general-N FP32 kernels: two CTAs per SM (default), phase-serial and
+# warp-specialised (RG_PLAIN_KERNEL=tiled[-serial|-ws] forces one)
+TILED_FORMS = ["two_cta", "serial", "ws"]
+TILED_ENV = {"two_cta": "tiled", "serial": "tiled-serial", "ws": "tiled-ws"}
+
+
+@pytest.mark.parametrize("form", TILED_FORMS)
+@pytest.mark.parametrize("n,horizon,M", [(65, 1, 20000), (100, 3, 8000), (129, 1, 8000), (257, 1, 3001),
+                                         (300, 2, 3000), (513, 1, 1000), (600, 10, 1024), (768, 1, 700),
+                                         (700, 2, 33)])
+def test_tiled_per_path_parity(gpu, oracle, monkeypatch, form, n, horizon, M):
+    """General-N FP32 kernels == oracle FP64 restatement per path (sizes
+    cover 1-3 column blocks of either width, partial last blocks and a path
+    count that is not a multiple of the tile)."""
+    monkeypatch.setenv("RG_PLAIN_KERNEL", TILED_ENV[form])
     mu, sigma, w = _factor_case(n, 7 + n)
     x = 0.02 * math.sqrt(horizon)
     k, thr, seed = max(1, n // 10), -0.03, 99 + n
@@ -495,7 +506,29 @@ def test_aggregated_statistics_match_daily(gpu, oracle):
         assert abs(r["p_breach"] - cf["p_breach"]) < 3 * se
 
 
-def test_tiled_var_exact(gpu, oracle):
+@pytest.mark.parametrize("n,horizon", [(150, 1), (600, 10), (97, 2), (768, 1)])
+def test_tiled_forms_identical_per_path(gpu, monkeypatch, n, horizon):
+    """The three FP32 kernels evaluate every asset return with the same FMA
+    chain: S identical on every path, w.R within FP32 summation-order
+    rounding, counts equal."""
+    mu, sigma, w = _factor_case(n, 31 + n)
+    port = gpu.Portfolio(mu, sigma, w)
+    M, x, k, thr = 40_000, 0.02 * math.sqrt(horizon), max(1, n // 10), -0.03
+    out = {}
+    for form in TILED_FORMS:
+        monkeypatch.setenv("RG_PLAIN_KERNEL", TILED_ENV[form])
+        out[form] = _run_paths(gpu, port, M, 5, x, k, thr, horizon=horizon)
+    r0, S0, W0 = out["serial"]
+    for form in ("two_cta", "ws"):
+        r1, S1, W1 = out[form]
+        assert (S1 == S0).all(), form
+        assert np.max(np.abs(W1 - W0)) <= 2e-6, form
+        assert r1["crash_count"] == r0["crash_count"], form
+
+
+@pytest.mark.parametrize("form", TILED_FORMS)
+def test_tiled_var_exact(gpu, oracle, monkeypatch, form):
+    monkeypatch.setenv("RG_PLAIN_KERNEL", TILED_ENV[form])
     r, W, _ = _var_case(gpu, 300_000, 0.99, n=150)
     var, cvar, T = oracle.var_cvar(W, 0.99)
     assert r["var"] == var and abs(r["cvar"] - cvar) <= 1e-9 * abs(cvar)

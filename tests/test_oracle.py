@@ -201,7 +201,8 @@ def test_oracle_figures_fixture_belongs_to_the_workloads(oracle):
         cf = oracle.portfolio_closed_form(p.mu, p.sigma, p.weights, p.horizon, p.port_threshold, figs["alpha"])
         for key in ("p_breach", "var", "cvar", "mean", "sd"):
             assert abs(cf[key] - fig[key]) <= 1e-12 * max(1.0, abs(cf[key])), (name, key)
-        assert (fig["x"], fig["k"], fig["horizon"]) == (p.x, p.k, p.horizon)
+        assert (fig["x"], fig["k"], fig["horizon"], fig["port_threshold"]) == (p.x, p.k, p.horizon,
+                                                                                p.port_threshold)
     p = synth.five_factor_600(n_paths=1)
     rng = np.random.default_rng(600)
     mu, sigma, B, idio = synth.factor_sigma(rng, p.n, 5, 0.5 * 0.01)
