@@ -55,6 +55,22 @@ __device__ __forceinline__ uint4 rg_philox(uint4 c, const PhiloxKeys &k)
     return c;
 }
 
+// Two independent Philox4x32-10 blocks, rounds interleaved (the same words
+// as two rg_philox calls; more independent work per thread where few warps
+// share an SM).
+__device__ __forceinline__ void rg_philox2(uint4 &a, uint4 &b, const PhiloxKeys &k)
+{
+#pragma unroll
+    for (int r = 0; r < 10; r++) {
+        const uint64_t p0 = (uint64_t)0xD2511F53u * a.x, p1 = (uint64_t)0xCD9E8D57u * a.z;
+        const uint64_t q0 = (uint64_t)0xD2511F53u * b.x, q1 = (uint64_t)0xCD9E8D57u * b.z;
+        a = make_uint4((uint32_t)(p1 >> 32) ^ a.y ^ k.k0[r], (uint32_t)p1, (uint32_t)(p0 >> 32) ^ a.w ^ k.k1[r],
+                       (uint32_t)p0);
+        b = make_uint4((uint32_t)(q1 >> 32) ^ b.y ^ k.k0[r], (uint32_t)q1, (uint32_t)(q0 >> 32) ^ b.w ^ k.k1[r],
+                       (uint32_t)q0);
+    }
+}
+
 __device__ __forceinline__ float rg_lg2_approx(float x)
 {
     float y;

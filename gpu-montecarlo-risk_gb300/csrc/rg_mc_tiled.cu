@@ -1,9 +1,10 @@
 // Plain fused FP32 Monte Carlo kernels for any asset count (the general-N
 // counterpart of the N <= 64 kernel; the reference caps N at 64,
-// src/05-GPU/monte_carlos_cuda.cu:34,78-81).  Three forms, each described
-// at its definition: the two-CTA mc_tiled2_kernel (default), the
-// phase-serial mc_tiled_kernel (RG_PLAIN_KERNEL=serial) and the
-// warp-specialised mc_tiled_ws_kernel (RG_PLAIN_KERNEL=ws).
+// src/05-GPU/monte_carlos_cuda.cu:34,78-81).  Two forms: the phase-serial
+// mc_tiled_kernel (default) and the warp-specialised mc_tiled_ws_kernel
+// (RG_PLAIN_KERNEL=ws, described at its definition), kept for comparison:
+// at N = 600, H = 10 it measured 170 ms per 1e7 paths against 162 ms
+// (aggregated draws 149 against 110 ms).
 //
 // Phase-serial form: a CTA owns a tile of 64 paths at a time (grid-stride
 // over tiles):
@@ -33,13 +34,13 @@ namespace rg {
 
 static constexpr int kTP = 64;        // paths per tile
 static constexpr int kTN = 128;       // assets per column block
-static constexpr int kTK = 8;         // K slice staged per step
+static constexpr int kTK = 8;         // K slice staged per step (warp-specialised form)
 static constexpr int kTiledThreads = 256;
 
 struct TiledArgs {
     PlainArgs a;          // counters, thresholds, Philox keys, VaR fields
     const float *Lt;      // [kpad][npad] L^T, FP32, zero padded
-    int kpad;             // N rounded up to kTK
+    int kpad;             // N rounded up to 16 (tiled_kpad)
     int npad;             // N rounded up to 256 (a multiple of both column-block widths)
     int aggregated;       // 1: one N(0, H) draw per asset (sqrt(H) z)
     float sqrt_h;
@@ -53,15 +54,16 @@ __device__ __forceinline__ void cp_async16(void *smem, const void *gmem)
 __device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;"); }
 __device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_group 0;" ::: "memory"); }
 
-template <bool VAR>
+// KT: rows of L^T staged per step (16 where shared memory allows, else 8).
+template <bool VAR, int KT>
 __global__ void __launch_bounds__(kTiledThreads, 1) mc_tiled_kernel(const TiledArgs t)
 {
     extern __shared__ __align__(16) float smem[];
     const PlainArgs &a = t.a;
     const int kpad = t.kpad;
     float *Zs = smem;                                  // [kpad][kTP]
-    float *Ls = Zs + (size_t)kpad * kTP;               // [2][kTK][kTN]
-    int *partS = (int *)(Ls + 2 * kTK * kTN);          // [16][kTP]
+    float *Ls = Zs + (size_t)kpad * kTP;               // [2][KT][kTN]
+    int *partS = (int *)(Ls + 2 * KT * kTN);           // [16][kTP]
     float *partP = (float *)(partS + 16 * kTP);        // [16][kTP]
     __shared__ int totS[kTP];
     __shared__ float totP[kTP];
@@ -83,36 +85,58 @@ __global__ void __launch_bounds__(kTiledThreads, 1) mc_tiled_kernel(const TiledA
 
     for (long long tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
         const long long p0 = tile * kTP;
-        // ---- 1. normals into Zs[k][p]
+        // ---- 1. normals into Zs[k][p]: 4 threads per path, each drawing two
+        // quads (q, q + 4) at a time with their Philox rounds interleaved
+        // (8 warps per SM leave little other independent work)
         {
-            const int p = tid & (kTP - 1), r = tid >> 6; // 4 threads per path
+            const int p = tid & (kTP - 1), r = tid >> 6;
             const unsigned long long path = a.path0 + (unsigned long long)(p0 + p);
             const uint32_t plo = (uint32_t)path, phi = (uint32_t)(path >> 32);
-            for (int q = r; q < kpad / 4; q += 4) {
-                float4 z = make_float4(0.f, 0.f, 0.f, 0.f);
-                if (q < nq) {
-                    const int days = t.aggregated ? 1 : a.horizon;
-                    for (int d = 0; d < days; d++) {
-                        const uint4 wv = rg_philox(make_uint4((uint32_t)(d * nq + q), 0u, plo, phi), a.keys);
-                        float z0, z1, z2, z3;
-                        rg_box_muller(wv.x, wv.y, z0, z1);
-                        rg_box_muller(wv.z, wv.w, z2, z3);
-                        z.x += z0;
-                        z.y += z1;
-                        z.z += z2;
-                        z.w += z3;
-                    }
-                    if (t.aggregated) {
-                        z.x *= t.sqrt_h;
-                        z.y *= t.sqrt_h;
-                        z.z *= t.sqrt_h;
-                        z.w *= t.sqrt_h;
-                    }
+            const int days = t.aggregated ? 1 : a.horizon;
+            for (int q = r; q < kpad / 4; q += 8) {
+                const int q2 = q + 4;
+                const bool has2 = q2 < kpad / 4;
+                float4 z = make_float4(0.f, 0.f, 0.f, 0.f), y = make_float4(0.f, 0.f, 0.f, 0.f);
+                for (int d = 0; d < days; d++) {
+                    uint4 wa = make_uint4((uint32_t)(d * nq + q), 0u, plo, phi);
+                    uint4 wb = make_uint4((uint32_t)(d * nq + q2), 0u, plo, phi);
+                    rg_philox2(wa, wb, a.keys);
+                    float z0, z1, z2, z3, y0, y1, y2, y3;
+                    rg_box_muller(wa.x, wa.y, z0, z1);
+                    rg_box_muller(wa.z, wa.w, z2, z3);
+                    rg_box_muller(wb.x, wb.y, y0, y1);
+                    rg_box_muller(wb.z, wb.w, y2, y3);
+                    z.x += z0;
+                    z.y += z1;
+                    z.z += z2;
+                    z.w += z3;
+                    y.x += y0;
+                    y.y += y1;
+                    y.z += y2;
+                    y.w += y3;
                 }
+                if (t.aggregated) {
+                    z.x *= t.sqrt_h;
+                    z.y *= t.sqrt_h;
+                    z.z *= t.sqrt_h;
+                    z.w *= t.sqrt_h;
+                    y.x *= t.sqrt_h;
+                    y.y *= t.sqrt_h;
+                    y.z *= t.sqrt_h;
+                    y.w *= t.sqrt_h;
+                }
+                if (q >= nq) z = make_float4(0.f, 0.f, 0.f, 0.f); // padding rows
+                if (q2 >= nq) y = make_float4(0.f, 0.f, 0.f, 0.f);
                 Zs[(4 * q + 0) * kTP + p] = z.x;
                 Zs[(4 * q + 1) * kTP + p] = z.y;
                 Zs[(4 * q + 2) * kTP + p] = z.z;
                 Zs[(4 * q + 3) * kTP + p] = z.w;
+                if (has2) {
+                    Zs[(4 * q2 + 0) * kTP + p] = y.x;
+                    Zs[(4 * q2 + 1) * kTP + p] = y.y;
+                    Zs[(4 * q2 + 2) * kTP + p] = y.z;
+                    Zs[(4 * q2 + 3) * kTP + p] = y.w;
+                }
             }
         }
         if (tid < kTP) {
@@ -130,25 +154,29 @@ __global__ void __launch_bounds__(kTiledThreads, 1) mc_tiled_kernel(const TiledA
             for (int i = 0; i < 4; i++)
 #pragma unroll
                 for (int j = 0; j < 4; j++) acc[i][j] = make_float2(0.f, 0.f);
-            // stage slice 0
+            // stage slice 0 (8 rows x 32 float4 per pass)
             {
-                const int kk = tid >> 5, c4 = tid & 31; // 8 rows x 32 float4
-                cp_async16(&Ls[kk * kTN + 4 * c4], &t.Lt[(size_t)kk * t.npad + c0 + 4 * c4]);
+                const int kk = tid >> 5, c4 = tid & 31;
+#pragma unroll
+                for (int h = 0; h < KT; h += 8)
+                    cp_async16(&Ls[(kk + h) * kTN + 4 * c4], &t.Lt[(size_t)(kk + h) * t.npad + c0 + 4 * c4]);
                 cp_async_commit();
             }
             int buf = 0;
-            for (int k0 = 0; k0 < kmax; k0 += kTK) {
+            for (int k0 = 0; k0 < kmax; k0 += KT) {
                 cp_async_wait_all();
                 __syncthreads();
-                if (k0 + kTK < kmax) {
+                if (k0 + KT < kmax) {
                     const int kk = tid >> 5, c4 = tid & 31;
-                    cp_async16(&Ls[(buf ^ 1) * kTK * kTN + kk * kTN + 4 * c4],
-                               &t.Lt[(size_t)(k0 + kTK + kk) * t.npad + c0 + 4 * c4]);
+#pragma unroll
+                    for (int h = 0; h < KT; h += 8)
+                        cp_async16(&Ls[(buf ^ 1) * KT * kTN + (kk + h) * kTN + 4 * c4],
+                                   &t.Lt[(size_t)(k0 + KT + kk + h) * t.npad + c0 + 4 * c4]);
                     cp_async_commit();
                 }
-                const float *Lb = Ls + buf * kTK * kTN;
+                const float *Lb = Ls + buf * KT * kTN;
 #pragma unroll
-                for (int kk = 0; kk < kTK; kk++) {
+                for (int kk = 0; kk < KT; kk++) {
                     const float4 z = *reinterpret_cast<const float4 *>(&Zs[(k0 + kk) * kTP + 4 * pg]);
                     const float4 l0 = *reinterpret_cast<const float4 *>(&Lb[kk * kTN + 8 * ag]);
                     const float4 l1 = *reinterpret_cast<const float4 *>(&Lb[kk * kTN + 8 * ag + 4]);
@@ -447,217 +475,27 @@ __global__ void __launch_bounds__(kWsThreadsT, 1) mc_tiled_ws_kernel(const Tiled
     cta_flush(a, crash, breach, n_tail, tail_fx, sacc, VAR ? shist : nullptr, VAR);
 }
 
-// ---------------------------------------------------------------------------
-// Two-CTA form (the default): the phase-serial scheme on 32-path tiles with
-// 512 threads a CTA and two CTAs per SM, so that one CTA's normal
-// generation overlaps the other's GEMM (32 warps per SM, each CTA taking
-// its turns independently).
-//   1. normals: item (path p, quad q) -> Zs[4q .. 4q+3][p], 32 paths a row;
-//   2. GEMM over 256-asset column blocks: 4-path x 4-asset register tiles
-//      (packed __ffma2_rn), L^T slices (8 x 256) staged by cp.async, double
-//      buffered; warp w holds assets c0 + 16w .. c0 + 16w + 15 and stops its
-//      K loop at c0 + 16(w + 1) (lower triangle, about 4 % padding at N = 600);
-//      a warp whose assets are all >= N skips the block;
-//   3. per block, a thread's 4 x 4 returns -> crash counts and w.R partial
-//      sums, reduced over the warp's 4 asset groups by shuffles, then over
-//      the 16 warps in warp order by the path's own thread (deterministic).
-// Each asset's return is the same FMA chain in k order as in the other two
-// forms, so S per path is identical between them.  64 registers a thread.
-// Shared memory: 128 x Kpad bytes for Z (77 KB at N = 600) + 16 KB of L
-// staging + 4 KB of partials (+ 16 KB of VaR histogram); two CTAs per SM up
-// to N = 600 without the histogram, one CTA above (the launcher asks the
-// occupancy calculator).
-static constexpr int kDuP = 32;
-static constexpr int kDuTN = 256;
-static constexpr int kDuThreads = 512;
-static constexpr int kDuWarps = kDuThreads / 32;
-
-template <bool VAR>
-__global__ void __launch_bounds__(kDuThreads, 2) mc_tiled2_kernel(const TiledArgs t)
-{
-    extern __shared__ __align__(16) float smem[];
-    const PlainArgs &a = t.a;
-    const int kpad = t.kpad;
-    float *Zs = smem;                                  // [kpad][kDuP]
-    float *Ls = Zs + (size_t)kpad * kDuP;              // [2][kTK][kDuTN]
-    int *partS = (int *)(Ls + 2 * kTK * kDuTN);        // [kDuWarps][kDuP]
-    float *partP = (float *)(partS + kDuWarps * kDuP); // [kDuWarps][kDuP]
-    __shared__ unsigned long long sacc[4];
-    __shared__ unsigned int shist[VAR ? kVarHistBins + 2 : 1];
-
-    const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
-    if (tid < 4) sacc[tid] = 0ull;
-    if (VAR && a.var_mode == 2)
-        for (int i = tid; i < a.sel_bins + 2; i += blockDim.x) shist[i] = 0u;
-    int crash = 0, breach = 0, n_tail = 0;
-    long long tail_fx = 0;
-    const int n = a.n;
-    const int nq = (n + 3) >> 2;
-    const int ncb = (n + kDuTN - 1) / kDuTN;
-    const int days = t.aggregated ? 1 : a.horizon;
-    const int items = kDuP * (kpad / 4);
-    const int pg = tid & 7, ag = tid >> 3;     // paths 4pg..4pg+3; assets 4ag..4ag+3 of a block
-    const int sk = tid >> 6, sc = tid & 63;    // staging: row sk, columns 4sc..4sc+3
-    const long long ntiles = (a.n_paths + kDuP - 1) / kDuP;
-
-    for (long long tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
-        const long long p0 = tile * kDuP;
-        // ---- 1. normals into Zs[k][p]
-        for (int it = tid; it < items; it += kDuThreads) {
-            const int p = it & (kDuP - 1), q = it >> 5;
-            float4 z = make_float4(0.f, 0.f, 0.f, 0.f);
-            if (q < nq) {
-                const unsigned long long path = a.path0 + (unsigned long long)(p0 + p);
-                const uint32_t plo = (uint32_t)path, phi = (uint32_t)(path >> 32);
-                for (int d = 0; d < days; d++) {
-                    const uint4 wv = rg_philox(make_uint4((uint32_t)(d * nq + q), 0u, plo, phi), a.keys);
-                    float z0, z1, z2, z3;
-                    rg_box_muller(wv.x, wv.y, z0, z1);
-                    rg_box_muller(wv.z, wv.w, z2, z3);
-                    z.x += z0;
-                    z.y += z1;
-                    z.z += z2;
-                    z.w += z3;
-                }
-                if (t.aggregated) {
-                    z.x *= t.sqrt_h;
-                    z.y *= t.sqrt_h;
-                    z.z *= t.sqrt_h;
-                    z.w *= t.sqrt_h;
-                }
-            }
-            Zs[(4 * q + 0) * kDuP + p] = z.x;
-            Zs[(4 * q + 1) * kDuP + p] = z.y;
-            Zs[(4 * q + 2) * kDuP + p] = z.z;
-            Zs[(4 * q + 3) * kDuP + p] = z.w;
-        }
-        __syncthreads();
-
-        // ---- 2./3. column blocks
-        int totS = 0;      // threads 0..31: path p0 + tid
-        float totP = 0.f;
-        for (int cb = 0; cb < ncb; cb++) {
-            const int c0 = cb * kDuTN;
-            const int kmax = min(kpad, c0 + kDuTN);
-            const int wlo = c0 + 16 * warp;
-            const int kend = min(kpad, wlo + 16);
-            const bool active = wlo < n;
-            float2 acc[4][2];
-#pragma unroll
-            for (int i = 0; i < 4; i++) {
-                acc[i][0] = make_float2(0.f, 0.f);
-                acc[i][1] = make_float2(0.f, 0.f);
-            }
-            cp_async16(&Ls[sk * kDuTN + 4 * sc], &t.Lt[(size_t)sk * t.npad + c0 + 4 * sc]);
-            cp_async_commit();
-            int buf = 0;
-            for (int k0 = 0; k0 < kmax; k0 += kTK) {
-                cp_async_wait_all();
-                __syncthreads();
-                if (k0 + kTK < kmax) {
-                    cp_async16(&Ls[(buf ^ 1) * kTK * kDuTN + sk * kDuTN + 4 * sc],
-                               &t.Lt[(size_t)(k0 + kTK + sk) * t.npad + c0 + 4 * sc]);
-                    cp_async_commit();
-                }
-                if (active && k0 < kend) {
-                    const float *Lb = Ls + buf * kTK * kDuTN;
-#pragma unroll
-                    for (int kk = 0; kk < kTK; kk++) {
-                        const float4 z = *reinterpret_cast<const float4 *>(&Zs[(k0 + kk) * kDuP + 4 * pg]);
-                        const float4 l = *reinterpret_cast<const float4 *>(&Lb[kk * kDuTN + 4 * ag]);
-                        const float zz[4] = {z.x, z.y, z.z, z.w};
-#pragma unroll
-                        for (int i = 0; i < 4; i++) {
-                            const float2 zi = make_float2(zz[i], zz[i]);
-                            acc[i][0] = __ffma2_rn(make_float2(l.x, l.y), zi, acc[i][0]);
-                            acc[i][1] = __ffma2_rn(make_float2(l.z, l.w), zi, acc[i][1]);
-                        }
-                    }
-                }
-                buf ^= 1;
-            }
-            float hm[4], wt[4];
-#pragma unroll
-            for (int jj = 0; jj < 4; jj++) {
-                const int c = c0 + 4 * ag + jj;
-                hm[jj] = (c < n) ? (float)((double)a.horizon * a.mu64[c]) : 0.f;
-                wt[jj] = (c < n) ? a.w[c] : 0.f;
-            }
-#pragma unroll
-            for (int i = 0; i < 4; i++) {
-                int sv = 0;
-                float pw = 0.f;
-#pragma unroll
-                for (int jj = 0; jj < 2; jj++) {
-                    const int a0 = c0 + 4 * ag + 2 * jj;
-                    const float r0 = hm[2 * jj] + acc[i][jj].x;
-                    const float r1 = hm[2 * jj + 1] + acc[i][jj].y;
-                    sv += (a0 < n && r0 < a.neg_x) ? 1 : 0;
-                    sv += (a0 + 1 < n && r1 < a.neg_x) ? 1 : 0;
-                    pw = fmaf(wt[2 * jj], r0, pw);
-                    pw = fmaf(wt[2 * jj + 1], r1, pw);
-                }
-                sv += __shfl_xor_sync(0xffffffffu, sv, 8);
-                pw += __shfl_xor_sync(0xffffffffu, pw, 8);
-                sv += __shfl_xor_sync(0xffffffffu, sv, 16);
-                pw += __shfl_xor_sync(0xffffffffu, pw, 16);
-                if (lane < 8) {
-                    partS[warp * kDuP + 4 * pg + i] = sv;
-                    partP[warp * kDuP + 4 * pg + i] = pw;
-                }
-            }
-            __syncthreads();
-            if (tid < kDuP) {
-#pragma unroll
-                for (int w = 0; w < kDuWarps; w++) {
-                    totS += partS[w * kDuP + tid];
-                    totP += partP[w * kDuP + tid];
-                }
-            }
-            // partS / partP are rewritten only after the next block's first
-            // barrier; Ls only after this one
-        }
-        if (tid < kDuP) {
-            const long long p = p0 + tid;
-            if (p < a.n_paths) {
-                crash += (totS >= a.k) ? 1 : 0;
-                breach += (a.has_w && totP < a.port_thr) ? 1 : 0;
-                if (a.s_values) a.s_values[p] = totS;
-                if (a.port_values) a.port_values[p] = totP;
-                if (VAR) var_path(a, totP, shist, n_tail, tail_fx);
-            }
-        }
-        __syncthreads(); // Zs and the partials are rewritten by the next tile
-    }
-    cta_flush(a, crash, breach, n_tail, tail_fx, sacc, VAR ? shist : nullptr, VAR);
-}
-
-size_t tiled2_smem_bytes(int n)
-{
-    const int kpad = (n + kTK - 1) / kTK * kTK;
-    return sizeof(float) * ((size_t)kpad * kDuP + 2 * kTK * kDuTN + 2 * kDuWarps * kDuP);
-}
-
 int tiled_max_n() { return 768; }
 
-size_t tiled_smem_bytes(int n)
+size_t tiled_smem_bytes(int n, int kt)
 {
-    const int kpad = (n + kTK - 1) / kTK * kTK;
-    return sizeof(float) * ((size_t)kpad * kTP + 2 * kTK * kTN + 2 * 16 * kTP);
+    const int kpad = tiled_kpad(n);
+    return sizeof(float) * ((size_t)kpad * kTP + 2 * (size_t)kt * kTN + 2 * 16 * kTP);
 }
 
 size_t tiled_ws_smem_bytes(int n)
 {
-    const int kpad = (n + kTK - 1) / kTK * kTK;
+    const int kpad = tiled_kpad(n);
     return sizeof(float) * (2 * (size_t)kpad * kWsP + 2 * kTK * kWsTN + 2 * 8 * kWsP);
 }
 
 // npad is a multiple of both column-block widths (128 and 256)
 int tiled_npad(int n) { return (n + kWsTN - 1) / kWsTN * kWsTN; }
-int tiled_kpad(int n) { return (n + kTK - 1) / kTK * kTK; }
+// K padded to 16: a 16-row L^T slice never reads past the last row
+int tiled_kpad(int n) { return (n + 15) / 16 * 16; }
 
-// The two-CTA kernel unless RG_PLAIN_KERNEL names "ws" (warp-specialised)
-// or "serial" (phase-serial, 64-path tiles, one CTA per SM).
+// The phase-serial kernel unless RG_PLAIN_KERNEL names "ws" (the
+// warp-specialised kernel, kept for comparison: it measured slower).
 cudaError_t launch_tiled(const PlainArgs &a, const float *Lt, bool aggregated, int sm_count,
                          cudaStream_t s)
 {
@@ -672,22 +510,6 @@ cudaError_t launch_tiled(const PlainArgs &a, const float *Lt, bool aggregated, i
     t.sqrt_h = sqrtf((float)a.horizon);
     const char *env = getenv("RG_PLAIN_KERNEL");
     const bool ws = env && strstr(env, "ws") != nullptr;
-    const bool serial = env && strstr(env, "serial") != nullptr;
-    if (!ws && !serial) {
-        const size_t smem = tiled2_smem_bytes(a.n);
-        auto kern = (a.var_mode != 0) ? mc_tiled2_kernel<true> : mc_tiled2_kernel<false>;
-        cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-        if (e != cudaSuccess) return e;
-        int per_sm = 0;
-        e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, kDuThreads, smem);
-        if (e != cudaSuccess) return e;
-        if (per_sm < 1) per_sm = 1;
-        long long tiles = (a.n_paths + kDuP - 1) / kDuP;
-        long long grid = (long long)sm_count * per_sm;
-        if (tiles < grid) grid = tiles;
-        kern<<<(unsigned)grid, kDuThreads, smem, s>>>(t);
-        return cudaGetLastError();
-    }
     if (ws) {
         const size_t smem = tiled_ws_smem_bytes(a.n);
         auto kern = (a.var_mode != 0) ? mc_tiled_ws_kernel<true> : mc_tiled_ws_kernel<false>;
@@ -699,9 +521,17 @@ cudaError_t launch_tiled(const PlainArgs &a, const float *Lt, bool aggregated, i
         kern<<<(unsigned)grid, kWsThreadsT, smem, s>>>(t);
         return cudaGetLastError();
     }
-    const size_t smem = tiled_smem_bytes(a.n);
-    auto kern = (a.var_mode != 0) ? mc_tiled_kernel<true> : mc_tiled_kernel<false>;
-    cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    // 16-row slices where the CTA's shared memory (dynamic + static) fits
+    int dev = 0, optin = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e == cudaSuccess) e = cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
+    if (e != cudaSuccess) return e;
+    const size_t static_bytes = 1024 + (a.var_mode != 0 ? 4 * (size_t)(kVarHistBins + 2) : 0);
+    const bool kt16 = tiled_smem_bytes(a.n, 16) + static_bytes <= (size_t)optin;
+    const size_t smem = tiled_smem_bytes(a.n, kt16 ? 16 : 8);
+    auto kern = (a.var_mode != 0) ? (kt16 ? mc_tiled_kernel<true, 16> : mc_tiled_kernel<true, 8>)
+                                  : (kt16 ? mc_tiled_kernel<false, 16> : mc_tiled_kernel<false, 8>);
+    e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess) return e;
     long long tiles = (a.n_paths + kTP - 1) / kTP;
     long long grid = sm_count;
