@@ -250,6 +250,50 @@ __host__ __device__ __forceinline__ uint32_t sw128_offset(int r, int k)
     return (uint32_t)((r >> 3) * 1024 + (r & 7) * 128 + chunk * 16 + (k & 7) * 2);
 }
 
+// Normals of quad q of one path summed over `days` draws (Philox counter
+// (d * nq + q, 0, path lo, path hi)); the paired form draws two quads of
+// two paths with their Philox rounds interleaved and gives the same sums.
+__device__ __forceinline__ float4 tc_quad_sum(int q, int nq, int days, uint32_t plo, uint32_t phi,
+                                              const PhiloxKeys &keys)
+{
+    float4 z = make_float4(0.f, 0.f, 0.f, 0.f);
+    for (int d = 0; d < days; d++) {
+        const uint4 wv = rg_philox(make_uint4((uint32_t)(d * nq + q), 0u, plo, phi), keys);
+        float z0, z1, z2, z3;
+        rg_box_muller(wv.x, wv.y, z0, z1);
+        rg_box_muller(wv.z, wv.w, z2, z3);
+        z.x += z0;
+        z.y += z1;
+        z.z += z2;
+        z.w += z3;
+    }
+    return z;
+}
+__device__ __forceinline__ void tc_quad_sum2(int q, uint32_t plo, uint32_t phi, int q2, uint32_t plo2, uint32_t phi2,
+                                             int nq, int days, const PhiloxKeys &keys, float4 &z, float4 &y)
+{
+    z = make_float4(0.f, 0.f, 0.f, 0.f);
+    y = make_float4(0.f, 0.f, 0.f, 0.f);
+    for (int d = 0; d < days; d++) {
+        uint4 wa = make_uint4((uint32_t)(d * nq + q), 0u, plo, phi);
+        uint4 wb = make_uint4((uint32_t)(d * nq + q2), 0u, plo2, phi2);
+        rg_philox2(wa, wb, keys);
+        float z0, z1, z2, z3, y0, y1, y2, y3;
+        rg_box_muller(wa.x, wa.y, z0, z1);
+        rg_box_muller(wa.z, wa.w, z2, z3);
+        rg_box_muller(wb.x, wb.y, y0, y1);
+        rg_box_muller(wb.z, wb.w, y2, y3);
+        z.x += z0;
+        z.y += z1;
+        z.z += z2;
+        z.w += z3;
+        y.x += y0;
+        y.y += y1;
+        y.z += y2;
+        y.w += y3;
+    }
+}
+
 __device__ __forceinline__ void split2(float v, int bf16, unsigned short &hi, unsigned short &lo)
 {
     if (bf16) {
@@ -773,33 +817,45 @@ __global__ void __launch_bounds__(kWsThreads, 1) mc_tcws_kernel(const __grid_con
                 // assigned round robin over the whole tile (i % kWsGenThreads == gtid)
                 int first = gtid - (kt * per_kt) % kWsGenThreads;
                 if (first < 0) first += kWsGenThreads;
-                for (int item = first; item < per_kt; item += kWsGenThreads) {
+                // two items at a time (item, item + kWsGenThreads), their
+                // Philox rounds interleaved when both are real quads
+                const int days = it.aggregated ? 1 : it.horizon;
+                for (int item = first; item < per_kt; item += 2 * kWsGenThreads) {
+                    const int item2 = item + kWsGenThreads;
+                    const bool two = item2 < per_kt;
                     const int ql = item / P, p = item - ql * P, q = kt * (kTcKt / 4) + ql;
+                    const int ql2 = two ? item2 / P : ql, p2 = two ? item2 - ql2 * P : p;
+                    const int q2 = kt * (kTcKt / 4) + ql2;
                     const unsigned long long path = it.path0 + (unsigned long long)(p0 + p);
+                    const unsigned long long path2 = it.path0 + (unsigned long long)(p0 + p2);
                     const uint32_t plo = (uint32_t)path, phi = (uint32_t)(path >> 32);
-                    float z[4] = {0.f, 0.f, 0.f, 0.f};
-                    if (q < nq) {
-                        const int days = it.aggregated ? 1 : it.horizon;
-                        for (int d = 0; d < days; d++) {
-                            const uint4 wv = rg_philox(make_uint4((uint32_t)(d * nq + q), 0u, plo, phi), it.keys);
-                            float z0, z1, z2, z3;
-                            rg_box_muller(wv.x, wv.y, z0, z1);
-                            rg_box_muller(wv.z, wv.w, z2, z3);
-                            z[0] += z0;
-                            z[1] += z1;
-                            z[2] += z2;
-                            z[3] += z3;
-                        }
-                        if (it.aggregated)
-                            for (int e = 0; e < 4; e++) z[e] *= it.sqrt_h;
+                    const uint32_t plo2 = (uint32_t)path2, phi2 = (uint32_t)(path2 >> 32);
+                    const bool real1 = q < nq, real2 = two && q2 < nq;
+                    float4 z = make_float4(0.f, 0.f, 0.f, 0.f), y = make_float4(0.f, 0.f, 0.f, 0.f);
+                    if (real1 && real2) tc_quad_sum2(q, plo, phi, q2, plo2, phi2, nq, days, it.keys, z, y);
+                    else if (real1) z = tc_quad_sum(q, nq, days, plo, phi, it.keys);
+                    else if (real2) y = tc_quad_sum(q2, nq, days, plo2, phi2, it.keys);
+                    if (it.aggregated) {
+                        z.x *= it.sqrt_h;
+                        z.y *= it.sqrt_h;
+                        z.z *= it.sqrt_h;
+                        z.w *= it.sqrt_h;
+                        y.x *= it.sqrt_h;
+                        y.y *= it.sqrt_h;
+                        y.z *= it.sqrt_h;
+                        y.w *= it.sqrt_h;
                     }
-                    unsigned short h[4], l[4];
-                    for (int e = 0; e < 4; e++) split2(z[e], it.bf16, h[e], l[e]);
-                    const uint32_t off = (uint32_t)zs * kZB + sw128_offset(p, 4 * ql);
-                    *reinterpret_cast<uint2 *>(zhi + off) =
-                        make_uint2((uint32_t)h[0] | ((uint32_t)h[1] << 16), (uint32_t)h[2] | ((uint32_t)h[3] << 16));
-                    *reinterpret_cast<uint2 *>(zlo + off) =
-                        make_uint2((uint32_t)l[0] | ((uint32_t)l[1] << 16), (uint32_t)l[2] | ((uint32_t)l[3] << 16));
+                    for (int u = 0; u < (two ? 2 : 1); u++) {
+                        const float4 v = u ? y : z;
+                        const float zz[4] = {v.x, v.y, v.z, v.w};
+                        unsigned short h[4], l[4];
+                        for (int e = 0; e < 4; e++) split2(zz[e], it.bf16, h[e], l[e]);
+                        const uint32_t off = (uint32_t)zs * kZB + sw128_offset(u ? p2 : p, 4 * (u ? ql2 : ql));
+                        *reinterpret_cast<uint2 *>(zhi + off) =
+                            make_uint2((uint32_t)h[0] | ((uint32_t)h[1] << 16), (uint32_t)h[2] | ((uint32_t)h[3] << 16));
+                        *reinterpret_cast<uint2 *>(zlo + off) =
+                            make_uint2((uint32_t)l[0] | ((uint32_t)l[1] << 16), (uint32_t)l[2] | ((uint32_t)l[3] << 16));
+                    }
                 }
                 fence_async_shared(); // this thread's writes -> async proxy (tensor cores)
                 mbar_arrive(&zfull[zs]);

@@ -55,16 +55,23 @@ __device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commi
 __device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_group 0;" ::: "memory"); }
 
 // KT: rows of L^T staged per step (16 where shared memory allows, else 8).
-template <bool VAR, int KT>
-__global__ void __launch_bounds__(kTiledThreads, 1) mc_tiled_kernel(const TiledArgs t)
+// THREADS: 256 (8 warps, 128-asset column blocks).  The kernel is also
+// correct with 512 (16 warps, 256-asset blocks), which measured slower at
+// N = 600, H = 10 (139 against 137 ms per 1e7 paths; aggregated draws 99
+// against 94 ms), so the launcher uses 256.
+template <bool VAR, int KT, int THREADS>
+__global__ void __launch_bounds__(THREADS, 1) mc_tiled_kernel(const TiledArgs t)
 {
+    constexpr int TN = THREADS / 2;   // assets per column block (8 per thread column)
+    constexpr int NAG = THREADS / 16; // asset groups of 8
+    constexpr int R = THREADS / 64;   // threads per path in the normal draws
     extern __shared__ __align__(16) float smem[];
     const PlainArgs &a = t.a;
     const int kpad = t.kpad;
     float *Zs = smem;                                  // [kpad][kTP]
-    float *Ls = Zs + (size_t)kpad * kTP;               // [2][KT][kTN]
-    int *partS = (int *)(Ls + 2 * KT * kTN);           // [16][kTP]
-    float *partP = (float *)(partS + 16 * kTP);        // [16][kTP]
+    float *Ls = Zs + (size_t)kpad * kTP;               // [2][KT][TN]
+    int *partS = (int *)(Ls + 2 * KT * TN);            // [NAG][kTP]
+    float *partP = (float *)(partS + NAG * kTP);       // [NAG][kTP]
     __shared__ int totS[kTP];
     __shared__ float totP[kTP];
     __shared__ unsigned long long sacc[4];
@@ -78,23 +85,23 @@ __global__ void __launch_bounds__(kTiledThreads, 1) mc_tiled_kernel(const TiledA
     long long tail_fx = 0;
     const int n = a.n;
     const int nq = (n + 3) >> 2;
-    const int ncb = (n + kTN - 1) / kTN;
+    const int ncb = (n + TN - 1) / TN;
     // register tile: paths 4*pg .. 4*pg+3, assets 8*ag .. 8*ag+7 of a block
     const int pg = tid & 15, ag = tid >> 4;
     const long long ntiles = (a.n_paths + kTP - 1) / kTP;
 
     for (long long tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
         const long long p0 = tile * kTP;
-        // ---- 1. normals into Zs[k][p]: 4 threads per path, each drawing two
-        // quads (q, q + 4) at a time with their Philox rounds interleaved
-        // (8 warps per SM leave little other independent work)
+        // ---- 1. normals into Zs[k][p]: R threads per path, each drawing two
+        // quads (q, q + R) at a time with their Philox rounds interleaved
+        // (8 or 16 warps per SM leave little other independent work)
         {
             const int p = tid & (kTP - 1), r = tid >> 6;
             const unsigned long long path = a.path0 + (unsigned long long)(p0 + p);
             const uint32_t plo = (uint32_t)path, phi = (uint32_t)(path >> 32);
             const int days = t.aggregated ? 1 : a.horizon;
-            for (int q = r; q < kpad / 4; q += 8) {
-                const int q2 = q + 4;
+            for (int q = r; q < kpad / 4; q += 2 * R) {
+                const int q2 = q + R;
                 const bool has2 = q2 < kpad / 4;
                 float4 z = make_float4(0.f, 0.f, 0.f, 0.f), y = make_float4(0.f, 0.f, 0.f, 0.f);
                 for (int d = 0; d < days; d++) {
@@ -147,19 +154,25 @@ __global__ void __launch_bounds__(kTiledThreads, 1) mc_tiled_kernel(const TiledA
 
         // ---- 2./3. column blocks
         for (int cb = 0; cb < ncb; cb++) {
-            const int c0 = cb * kTN;
-            const int kmax = min(kpad, c0 + kTN);
+            const int c0 = cb * TN;
+            const int kmax = min(kpad, c0 + TN);
+            // warp w holds assets c0 + 16w .. c0 + 16w + 15 (ag = 2w, 2w + 1):
+            // L[c][k] = 0 for k > c, so its multiply-adds stop at c0 + 16(w + 1)
+            // (the skipped terms are exact zeros; the block's staging and
+            // barriers still run for every warp)
+            const int kend_w = min(kmax, c0 + 16 * ((tid >> 5) + 1));
+            const bool live_w = c0 + 16 * (tid >> 5) < n;
             float2 acc[4][4];
 #pragma unroll
             for (int i = 0; i < 4; i++)
 #pragma unroll
                 for (int j = 0; j < 4; j++) acc[i][j] = make_float2(0.f, 0.f);
-            // stage slice 0 (8 rows x 32 float4 per pass)
+            // stage slice 0 (8 rows x TN / 4 float4 per pass)
             {
-                const int kk = tid >> 5, c4 = tid & 31;
+                const int kk = tid / (TN / 4), c4 = tid % (TN / 4);
 #pragma unroll
                 for (int h = 0; h < KT; h += 8)
-                    cp_async16(&Ls[(kk + h) * kTN + 4 * c4], &t.Lt[(size_t)(kk + h) * t.npad + c0 + 4 * c4]);
+                    cp_async16(&Ls[(kk + h) * TN + 4 * c4], &t.Lt[(size_t)(kk + h) * t.npad + c0 + 4 * c4]);
                 cp_async_commit();
             }
             int buf = 0;
@@ -167,27 +180,29 @@ __global__ void __launch_bounds__(kTiledThreads, 1) mc_tiled_kernel(const TiledA
                 cp_async_wait_all();
                 __syncthreads();
                 if (k0 + KT < kmax) {
-                    const int kk = tid >> 5, c4 = tid & 31;
+                    const int kk = tid / (TN / 4), c4 = tid % (TN / 4);
 #pragma unroll
                     for (int h = 0; h < KT; h += 8)
-                        cp_async16(&Ls[(buf ^ 1) * KT * kTN + (kk + h) * kTN + 4 * c4],
+                        cp_async16(&Ls[(buf ^ 1) * KT * TN + (kk + h) * TN + 4 * c4],
                                    &t.Lt[(size_t)(k0 + KT + kk + h) * t.npad + c0 + 4 * c4]);
                     cp_async_commit();
                 }
-                const float *Lb = Ls + buf * KT * kTN;
+                const float *Lb = Ls + buf * KT * TN;
+                if (live_w && k0 < kend_w) {
 #pragma unroll
-                for (int kk = 0; kk < KT; kk++) {
-                    const float4 z = *reinterpret_cast<const float4 *>(&Zs[(k0 + kk) * kTP + 4 * pg]);
-                    const float4 l0 = *reinterpret_cast<const float4 *>(&Lb[kk * kTN + 8 * ag]);
-                    const float4 l1 = *reinterpret_cast<const float4 *>(&Lb[kk * kTN + 8 * ag + 4]);
-                    const float zz[4] = {z.x, z.y, z.z, z.w};
+                    for (int kk = 0; kk < KT; kk++) {
+                        const float4 z = *reinterpret_cast<const float4 *>(&Zs[(k0 + kk) * kTP + 4 * pg]);
+                        const float4 l0 = *reinterpret_cast<const float4 *>(&Lb[kk * TN + 8 * ag]);
+                        const float4 l1 = *reinterpret_cast<const float4 *>(&Lb[kk * TN + 8 * ag + 4]);
+                        const float zz[4] = {z.x, z.y, z.z, z.w};
 #pragma unroll
-                    for (int i = 0; i < 4; i++) {
-                        const float2 zi = make_float2(zz[i], zz[i]);
-                        acc[i][0] = __ffma2_rn(make_float2(l0.x, l0.y), zi, acc[i][0]);
-                        acc[i][1] = __ffma2_rn(make_float2(l0.z, l0.w), zi, acc[i][1]);
-                        acc[i][2] = __ffma2_rn(make_float2(l1.x, l1.y), zi, acc[i][2]);
-                        acc[i][3] = __ffma2_rn(make_float2(l1.z, l1.w), zi, acc[i][3]);
+                        for (int i = 0; i < 4; i++) {
+                            const float2 zi = make_float2(zz[i], zz[i]);
+                            acc[i][0] = __ffma2_rn(make_float2(l0.x, l0.y), zi, acc[i][0]);
+                            acc[i][1] = __ffma2_rn(make_float2(l0.z, l0.w), zi, acc[i][1]);
+                            acc[i][2] = __ffma2_rn(make_float2(l1.x, l1.y), zi, acc[i][2]);
+                            acc[i][3] = __ffma2_rn(make_float2(l1.z, l1.w), zi, acc[i][3]);
+                        }
                     }
                 }
                 buf ^= 1;
@@ -222,7 +237,7 @@ __global__ void __launch_bounds__(kTiledThreads, 1) mc_tiled_kernel(const TiledA
                 int s = totS[tid];
                 float pw = totP[tid];
 #pragma unroll
-                for (int g = 0; g < 16; g++) {
+                for (int g = 0; g < NAG; g++) {
                     s += partS[g * kTP + tid];
                     pw += partP[g * kTP + tid];
                 }
@@ -477,10 +492,10 @@ __global__ void __launch_bounds__(kWsThreadsT, 1) mc_tiled_ws_kernel(const Tiled
 
 int tiled_max_n() { return 768; }
 
-size_t tiled_smem_bytes(int n, int kt)
+size_t tiled_smem_bytes(int n, int kt, int threads)
 {
     const int kpad = tiled_kpad(n);
-    return sizeof(float) * ((size_t)kpad * kTP + 2 * (size_t)kt * kTN + 2 * 16 * kTP);
+    return sizeof(float) * ((size_t)kpad * kTP + 2 * (size_t)kt * (threads / 2) + 2 * (size_t)(threads / 16) * kTP);
 }
 
 size_t tiled_ws_smem_bytes(int n)
@@ -521,22 +536,26 @@ cudaError_t launch_tiled(const PlainArgs &a, const float *Lt, bool aggregated, i
         kern<<<(unsigned)grid, kWsThreadsT, smem, s>>>(t);
         return cudaGetLastError();
     }
-    // 16-row slices where the CTA's shared memory (dynamic + static) fits
+    // 16-row L^T slices where the CTA's shared memory (dynamic + static)
+    // fits, else 8
     int dev = 0, optin = 0;
     cudaError_t e = cudaGetDevice(&dev);
     if (e == cudaSuccess) e = cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
     if (e != cudaSuccess) return e;
-    const size_t static_bytes = 1024 + (a.var_mode != 0 ? 4 * (size_t)(kVarHistBins + 2) : 0);
-    const bool kt16 = tiled_smem_bytes(a.n, 16) + static_bytes <= (size_t)optin;
-    const size_t smem = tiled_smem_bytes(a.n, kt16 ? 16 : 8);
-    auto kern = (a.var_mode != 0) ? (kt16 ? mc_tiled_kernel<true, 16> : mc_tiled_kernel<true, 8>)
-                                  : (kt16 ? mc_tiled_kernel<false, 16> : mc_tiled_kernel<false, 8>);
+    const bool var = a.var_mode != 0;
+    const size_t static_bytes = 1024 + (var ? 4 * (size_t)(kVarHistBins + 2) : 0);
+    const int threads = kTiledThreads;
+    const bool kt16 = tiled_smem_bytes(a.n, 16, threads) + static_bytes <= (size_t)optin;
+    const size_t smem = tiled_smem_bytes(a.n, kt16 ? 16 : 8, threads);
+    void (*kern)(const TiledArgs) =
+        var ? (kt16 ? mc_tiled_kernel<true, 16, kTiledThreads> : mc_tiled_kernel<true, 8, kTiledThreads>)
+            : (kt16 ? mc_tiled_kernel<false, 16, kTiledThreads> : mc_tiled_kernel<false, 8, kTiledThreads>);
     e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess) return e;
     long long tiles = (a.n_paths + kTP - 1) / kTP;
     long long grid = sm_count;
     if (tiles < grid) grid = tiles;
-    kern<<<(unsigned)grid, kTiledThreads, smem, s>>>(t);
+    kern<<<(unsigned)grid, threads, smem, s>>>(t);
     return cudaGetLastError();
 }
 
