@@ -38,22 +38,24 @@ struct ConstBlock {
 };
 
 // Normals of quad q of one path, summed over the horizon.
+// `second` = false skips the second Box-Muller pair (the last quad when
+// N mod 4 is 1 or 2: those normals feed only padding rows).
 template <int NQ, bool ONE_DAY>
 __device__ __forceinline__ float4 fused_quad_normals(int q, int horizon, uint32_t plo, uint32_t phi,
-                                                     const PhiloxKeys &keys)
+                                                     const PhiloxKeys &keys, bool second = true)
 {
-    float4 z;
+    float4 z = make_float4(0.f, 0.f, 0.f, 0.f);
     {
         const uint4 w = rg_philox(make_uint4((uint32_t)q, 0u, plo, phi), keys);
         rg_box_muller(w.x, w.y, z.x, z.y);
-        rg_box_muller(w.z, w.w, z.z, z.w);
+        if (second) rg_box_muller(w.z, w.w, z.z, z.w);
     }
     if (!ONE_DAY) {
         for (int d = 1; d < horizon; d++) {
             const uint4 w = rg_philox(make_uint4((uint32_t)(d * NQ + q), 0u, plo, phi), keys);
-            float z0, z1, z2, z3;
+            float z0, z1, z2 = 0.f, z3 = 0.f;
             rg_box_muller(w.x, w.y, z0, z1);
-            rg_box_muller(w.z, w.w, z2, z3);
+            if (second) rg_box_muller(w.z, w.w, z2, z3);
             z.x += z0;
             z.y += z1;
             z.z += z2;
@@ -149,6 +151,9 @@ __global__ void __launch_bounds__(kFusedThreads, ONE_DAY ? 4 : 3) mc_rows_kernel
     long long tail_fx = 0;
 
     const int n = a.n;
+    // rows of the last group that exist (1..4): the others are skipped
+    // (uniform across the grid, so the branches do not diverge)
+    const int last_rows = n - 4 * (NQ - 1);
     int crash = 0, breach = 0;
     const long long stride = (long long)gridDim.x * blockDim.x;
     for (long long p = (long long)blockIdx.x * blockDim.x + tid; p < a.n_paths; p += stride) {
@@ -156,7 +161,7 @@ __global__ void __launch_bounds__(kFusedThreads, ONE_DAY ? 4 : 3) mc_rows_kernel
         const uint32_t plo = (uint32_t)path, phi = (uint32_t)(path >> 32);
         float2 z2[2 * NQ];
         {
-            const float4 z = fused_quad_normals<NQ, ONE_DAY>(0, a.horizon, plo, phi, a.keys);
+            const float4 z = fused_quad_normals<NQ, ONE_DAY>(0, a.horizon, plo, phi, a.keys, NQ > 1 || last_rows > 2);
             z2[0] = make_float2(z.x, z.y);
             z2[1] = make_float2(z.z, z.w);
         }
@@ -165,28 +170,43 @@ __global__ void __launch_bounds__(kFusedThreads, ONE_DAY ? 4 : 3) mc_rows_kernel
 #pragma unroll
         for (int g = 0; g < NQ; g++) {
             if (g + 1 < NQ) {
-                const float4 z = fused_quad_normals<NQ, ONE_DAY>(g + 1, a.horizon, plo, phi, a.keys);
+                const float4 z = fused_quad_normals<NQ, ONE_DAY>(g + 1, a.horizon, plo, phi, a.keys,
+                                                                 g + 2 < NQ || last_rows > 2);
                 z2[2 * g + 2] = make_float2(z.x, z.y);
                 z2[2 * g + 3] = make_float2(z.z, z.w);
             }
             float2 acc[4];
 #pragma unroll
             for (int e = 0; e < 4; e++) acc[e] = make_float2(0.f, 0.f);
+            if (g < NQ - 1) {
 #pragma unroll
-            for (int q = 0; q <= g; q++) {
+                for (int q = 0; q <= g; q++) {
+#pragma unroll
+                    for (int e = 0; e < 4; e++) {
+                        const float4 l = cb.L[packed_row_offset(4 * g + e) / 4 + q];
+                        acc[e] = __ffma2_rn(make_float2(l.x, l.y), z2[2 * q], acc[e]);
+                        acc[e] = __ffma2_rn(make_float2(l.z, l.w), z2[2 * q + 1], acc[e]);
+                    }
+                }
+            } else {
+                // last group: rows >= N are padding (same FMA order per row)
 #pragma unroll
                 for (int e = 0; e < 4; e++) {
-                    const float4 l = cb.L[packed_row_offset(4 * g + e) / 4 + q];
-                    acc[e] = __ffma2_rn(make_float2(l.x, l.y), z2[2 * q], acc[e]);
-                    acc[e] = __ffma2_rn(make_float2(l.z, l.w), z2[2 * q + 1], acc[e]);
+                    if (e < last_rows) {
+#pragma unroll
+                        for (int q = 0; q <= g; q++) {
+                            const float4 l = cb.L[packed_row_offset(4 * g + e) / 4 + q];
+                            acc[e] = __ffma2_rn(make_float2(l.x, l.y), z2[2 * q], acc[e]);
+                            acc[e] = __ffma2_rn(make_float2(l.z, l.w), z2[2 * q + 1], acc[e]);
+                        }
+                    }
                 }
             }
 #pragma unroll
             for (int e = 0; e < 4; e++) {
-                const int i = 4 * g + e;
+                if (g == NQ - 1 && e >= last_rows) continue;
                 const float r = (&cb.hmu[g].x)[e] + (acc[e].x + acc[e].y);
-                const bool hit = (r < a.neg_x) && (g < NQ - 1 || i < n);
-                S += hit ? 1 : 0;
+                S += (r < a.neg_x) ? 1 : 0;
                 port = fmaf((&cb.w[g].x)[e], r, port);
             }
         }
