@@ -75,6 +75,13 @@ ORACLE_FIGURES = os.path.join(ROOT, "tests", "golden", "oracle_figures.json")
 #   mc_tcws_kernel at N = 600: the Lhat tiles read once, about 1.0 MB
 NCU_TRAFFIC_BYTES = {"one_factor_50": 42_496, "five_factor_600": 1_000_000}
 
+# Thread instructions the tcgen05 kernel issues per normal it draws, daily
+# draws at N = 600, H = 10 (ncu smsp__inst_executed.sum of a 1e6-path launch,
+# 3.996e9 warp instructions x 32 / 6e9 normals).  With the SM count and the
+# sampled SM clock it gives the kernel's issue bound: every SM issuing 4 warp
+# instructions (128 thread instructions) a cycle.
+TC_THREAD_INST_PER_NORMAL = 21.3
+
 
 def parse():
     ap = argparse.ArgumentParser()
@@ -703,6 +710,14 @@ def engine_arm(args):
                                "issued_tflops_dense_x3": 3 * 2 * n * n * count / (ms_per_step * 1e-3) / 1e12},
                     "algorithmic_flops_per_path": flops_per_path, "normals_per_path": normals_per_path,
                     "traffic": NCU_TRAFFIC_BYTES.get(key)}
+        if n == 600 and args.draw_mode == "daily":
+            sms = torch.cuda.get_device_properties(torch.cuda.current_device()).multi_processor_count
+            mhz = clk.get("sm_mhz") or 2070.0
+            bound = sms * 128 * mhz * 1e6 / TC_THREAD_INST_PER_NORMAL
+            roofline["issue_bound"] = {
+                "normals_per_s": bound, "frac": normals_per_s / bound,
+                "basis": f"{TC_THREAD_INST_PER_NORMAL} thread instructions per normal (ncu) at 128 a cycle on "
+                         f"each of {sms} SMs, {mhz:.0f} MHz"}
     else:
         t_ideal = (flops_per_path / (peaks["fp32_tflops"] * 1e12)
                    + normals_drawn / peaks["normals_per_s"]) * count
