@@ -1,10 +1,11 @@
 // Plain fused FP32 Monte Carlo kernels for any asset count (the general-N
 // counterpart of the N <= 64 kernel; the reference caps N at 64,
-// src/05-GPU/monte_carlos_cuda.cu:34,78-81).  Two forms: the phase-serial
-// mc_tiled_kernel (default) and the warp-specialised mc_tiled_ws_kernel
-// (RG_PLAIN_KERNEL=ws, described at its definition), kept for comparison:
-// at N = 600, H = 10 it measured 170 ms per 1e7 paths against 162 ms
-// (aggregated draws 149 against 110 ms).
+// src/05-GPU/monte_carlos_cuda.cu:34,78-81).  Three forms, each described
+// at its definition: the pipelined mc_tiled_pipe_kernel (default), the
+// phase-serial mc_tiled_kernel it is built from (RG_PLAIN_KERNEL=serial) and
+// the warp-specialised mc_tiled_ws_kernel (RG_PLAIN_KERNEL=ws).  At N = 600,
+// H = 10, 1e7 paths: 124.5, 136.6 and 170 ms with daily draws; 94.0, 94.1
+// and 149 ms with aggregated draws.
 //
 // Phase-serial form: a CTA owns a tile of 64 paths at a time (grid-stride
 // over tiles):
@@ -490,6 +491,236 @@ __global__ void __launch_bounds__(kWsThreadsT, 1) mc_tiled_ws_kernel(const Tiled
     cta_flush(a, crash, breach, n_tail, tail_fx, sacc, VAR ? shist : nullptr, VAR);
 }
 
+// ---------------------------------------------------------------------------
+// Pipelined form (the default): the phase-serial kernel's tile (64
+// paths, one Z buffer) with generation and GEMM on different warps of one
+// 512-thread CTA, overlapped through the 128-row ranges of Z.
+//   warps 0-7  GEMM: column blocks in DESCENDING order and, inside a block,
+//              K in DESCENDING order.  Block cb reads rows [0, 128(cb + 1)),
+//              its own range [128 cb, 128(cb + 1)) first; blocks below cb
+//              never read that range, so it is released (RELEASE[cb]) as soon
+//              as the block's K loop has passed it.  The next tile's first
+//              block (the top one) reads the ranges top down, the order in
+//              which they were released, waiting on FILLED[r] as it enters
+//              range r.
+//   warps 8-15 normals of the next tile, range by range from the top
+//              (waiting on RELEASE[r], then arriving on FILLED[r]); two quads
+//              at a time with their Philox rounds interleaved (rg_philox2).
+// At N = 600 the bottom range, released last, is needed only at the end of
+// the next tile's top block, so generation and GEMM overlap almost entirely.
+// The GEMM is the phase-serial kernel's (4-path x 8-asset FFMA2 tiles,
+// 16-row L^T slices staged by cp.async, per-warp triangle cut) with a
+// barrier among the GEMM warps only.  Each return is the same terms as in
+// the other forms, accumulated in descending k.
+// Named barriers, pairing by construction (both roles walk the same static
+// tile list and block count): 1 = GEMM warps (256); 2 + r = FILLED[r] (256
+// generator arrivals + 256 GEMM syncs, once a tile); 8 + r = RELEASE[r] (256
+// GEMM arrivals in every tile but the CTA's last + 256 generator syncs in
+// every tile but the first); r < 6 (N <= 768).
+static constexpr int kPipeThreads = 512;
+static constexpr int kPipeHalf = 256;
+
+template <bool VAR, int KT>
+__global__ void __launch_bounds__(kPipeThreads, 1) mc_tiled_pipe_kernel(const TiledArgs t)
+{
+    extern __shared__ __align__(16) float smem[];
+    const PlainArgs &a = t.a;
+    const int kpad = t.kpad;
+    float *Zs = smem;                                  // [kpad][kTP]
+    float *Ls = Zs + (size_t)kpad * kTP;               // [2][KT][kTN]
+    int *partS = (int *)(Ls + 2 * KT * kTN);           // [16][kTP]
+    float *partP = (float *)(partS + 16 * kTP);        // [16][kTP]
+    __shared__ unsigned long long sacc[4];
+    __shared__ unsigned int shist[VAR ? kVarHistBins + 2 : 1];
+
+    const int tid = threadIdx.x;
+    if (tid < 4) sacc[tid] = 0ull;
+    if (VAR && a.var_mode == 2)
+        for (int i = tid; i < a.sel_bins + 2; i += blockDim.x) shist[i] = 0u;
+    __syncthreads();
+    int crash = 0, breach = 0, n_tail = 0;
+    long long tail_fx = 0;
+    const int n = a.n;
+    const int nq = (n + 3) >> 2;
+    const int ncb = (n + kTN - 1) / kTN;
+    const long long ntiles = (a.n_paths + kTP - 1) / kTP;
+    const long long my_tiles = (long long)blockIdx.x < ntiles ? (ntiles - 1 - blockIdx.x) / gridDim.x + 1 : 0;
+
+    if (tid >= kPipeHalf) {
+        // ============================ generator ============================
+        const int gt = tid - kPipeHalf;
+        const int p = gt & (kTP - 1), r4 = gt >> 6; // 4 threads per path
+        const int days = t.aggregated ? 1 : a.horizon;
+        for (long long j = 0; j < my_tiles; j++) {
+            const long long p0 = ((long long)blockIdx.x + j * gridDim.x) * kTP;
+            const unsigned long long path = a.path0 + (unsigned long long)(p0 + p);
+            const uint32_t plo = (uint32_t)path, phi = (uint32_t)(path >> 32);
+            for (int r = ncb - 1; r >= 0; r--) {
+                if (j >= 1) nbar_sync(8 + r, kPipeThreads); // range r of the previous tile is dead
+                const int qlo = 32 * r, qhi = min(kpad / 4, 32 * r + 32);
+                for (int q = qlo + r4; q < qhi; q += 8) {
+                    const int q2 = q + 4;
+                    const bool has2 = q2 < qhi;
+                    float4 z = make_float4(0.f, 0.f, 0.f, 0.f), y = make_float4(0.f, 0.f, 0.f, 0.f);
+                    for (int d = 0; d < days; d++) {
+                        uint4 wa = make_uint4((uint32_t)(d * nq + q), 0u, plo, phi);
+                        uint4 wb = make_uint4((uint32_t)(d * nq + q2), 0u, plo, phi);
+                        rg_philox2(wa, wb, a.keys);
+                        float z0, z1, z2, z3, y0, y1, y2, y3;
+                        rg_box_muller(wa.x, wa.y, z0, z1);
+                        rg_box_muller(wa.z, wa.w, z2, z3);
+                        rg_box_muller(wb.x, wb.y, y0, y1);
+                        rg_box_muller(wb.z, wb.w, y2, y3);
+                        z.x += z0;
+                        z.y += z1;
+                        z.z += z2;
+                        z.w += z3;
+                        y.x += y0;
+                        y.y += y1;
+                        y.z += y2;
+                        y.w += y3;
+                    }
+                    if (t.aggregated) {
+                        z.x *= t.sqrt_h;
+                        z.y *= t.sqrt_h;
+                        z.z *= t.sqrt_h;
+                        z.w *= t.sqrt_h;
+                        y.x *= t.sqrt_h;
+                        y.y *= t.sqrt_h;
+                        y.z *= t.sqrt_h;
+                        y.w *= t.sqrt_h;
+                    }
+                    if (q >= nq) z = make_float4(0.f, 0.f, 0.f, 0.f); // padding rows
+                    if (q2 >= nq) y = make_float4(0.f, 0.f, 0.f, 0.f);
+                    Zs[(4 * q + 0) * kTP + p] = z.x;
+                    Zs[(4 * q + 1) * kTP + p] = z.y;
+                    Zs[(4 * q + 2) * kTP + p] = z.z;
+                    Zs[(4 * q + 3) * kTP + p] = z.w;
+                    if (has2) {
+                        Zs[(4 * q2 + 0) * kTP + p] = y.x;
+                        Zs[(4 * q2 + 1) * kTP + p] = y.y;
+                        Zs[(4 * q2 + 2) * kTP + p] = y.z;
+                        Zs[(4 * q2 + 3) * kTP + p] = y.w;
+                    }
+                }
+                __threadfence_block();
+                nbar_arrive(2 + r, kPipeThreads); // range r of this tile written
+            }
+        }
+    } else {
+        // ============================== GEMM ===============================
+        const int pg = tid & 15, ag = tid >> 4;
+        const int kk0 = tid >> 5, c4 = tid & 31; // staging: 8 rows x 32 float4 per pass
+        for (long long j = 0; j < my_tiles; j++) {
+            const long long p0 = ((long long)blockIdx.x + j * gridDim.x) * kTP;
+            const bool has_next = j + 1 < my_tiles;
+            int totS = 0;   // threads 0..63: path p0 + tid
+            float totP = 0.f;
+            for (int cb = ncb - 1; cb >= 0; cb--) {
+                const int c0 = cb * kTN;
+                const int kmax = min(kpad, c0 + kTN);
+                const int kend_w = min(kmax, c0 + 16 * ((tid >> 5) + 1));
+                const bool live_w = c0 + 16 * (tid >> 5) < n;
+                float2 acc[4][4];
+#pragma unroll
+                for (int i = 0; i < 4; i++)
+#pragma unroll
+                    for (int jj = 0; jj < 4; jj++) acc[i][jj] = make_float2(0.f, 0.f);
+                // K descending: slices kmax - KT, kmax - 2 KT, ..., 0
+                const int ktop = kmax - KT;
+#pragma unroll
+                for (int h = 0; h < KT; h += 8)
+                    cp_async16(&Ls[(kk0 + h) * kTN + 4 * c4], &t.Lt[(size_t)(ktop + kk0 + h) * t.npad + c0 + 4 * c4]);
+                cp_async_commit();
+                int buf = 0;
+                for (int k0 = ktop; k0 >= 0; k0 -= KT) {
+                    cp_async_wait_all();
+                    nbar_sync(1, kPipeHalf);
+                    // every GEMM warp is past slice k0 + KT: entering a new
+                    // range (k0 + KT a multiple of 128) releases the one above
+                    // it if that is this block's own range
+                    if (has_next && k0 + KT == c0) nbar_arrive(8 + cb, kPipeThreads);
+                    // the top block reads every range first in this tile
+                    if (cb == ncb - 1 && (k0 + KT) % kTN == 0 || (cb == ncb - 1 && k0 == ktop))
+                        nbar_sync(2 + k0 / kTN, kPipeThreads);
+                    if (k0 - KT >= 0) {
+#pragma unroll
+                        for (int h = 0; h < KT; h += 8)
+                            cp_async16(&Ls[(buf ^ 1) * KT * kTN + (kk0 + h) * kTN + 4 * c4],
+                                       &t.Lt[(size_t)(k0 - KT + kk0 + h) * t.npad + c0 + 4 * c4]);
+                        cp_async_commit();
+                    }
+                    const float *Lb = Ls + buf * KT * kTN;
+                    if (live_w && k0 < kend_w) {
+#pragma unroll
+                        for (int kk = KT - 1; kk >= 0; kk--) {
+                            const float4 z = *reinterpret_cast<const float4 *>(&Zs[(k0 + kk) * kTP + 4 * pg]);
+                            const float4 l0 = *reinterpret_cast<const float4 *>(&Lb[kk * kTN + 8 * ag]);
+                            const float4 l1 = *reinterpret_cast<const float4 *>(&Lb[kk * kTN + 8 * ag + 4]);
+                            const float zz[4] = {z.x, z.y, z.z, z.w};
+#pragma unroll
+                            for (int i = 0; i < 4; i++) {
+                                const float2 zi = make_float2(zz[i], zz[i]);
+                                acc[i][0] = __ffma2_rn(make_float2(l0.x, l0.y), zi, acc[i][0]);
+                                acc[i][1] = __ffma2_rn(make_float2(l0.z, l0.w), zi, acc[i][1]);
+                                acc[i][2] = __ffma2_rn(make_float2(l1.x, l1.y), zi, acc[i][2]);
+                                acc[i][3] = __ffma2_rn(make_float2(l1.z, l1.w), zi, acc[i][3]);
+                            }
+                        }
+                    }
+                    buf ^= 1;
+                }
+                float hm[8], wt[8];
+#pragma unroll
+                for (int jj = 0; jj < 8; jj++) {
+                    const int c = c0 + 8 * ag + jj;
+                    hm[jj] = (c < n) ? (float)((double)a.horizon * a.mu64[c]) : 0.f;
+                    wt[jj] = (c < n) ? a.w[c] : 0.f;
+                }
+#pragma unroll
+                for (int i = 0; i < 4; i++) {
+                    int sv = 0;
+                    float pw = 0.f;
+#pragma unroll
+                    for (int jj = 0; jj < 4; jj++) {
+                        const int a0 = c0 + 8 * ag + 2 * jj;
+                        const float r0 = hm[2 * jj] + acc[i][jj].x;
+                        const float r1 = hm[2 * jj + 1] + acc[i][jj].y;
+                        sv += (a0 < n && r0 < a.neg_x) ? 1 : 0;
+                        sv += (a0 + 1 < n && r1 < a.neg_x) ? 1 : 0;
+                        pw = fmaf(wt[2 * jj], r0, pw);
+                        pw = fmaf(wt[2 * jj + 1], r1, pw);
+                    }
+                    partS[ag * kTP + 4 * pg + i] = sv;
+                    partP[ag * kTP + 4 * pg + i] = pw;
+                }
+                nbar_sync(1, kPipeHalf); // every GEMM warp is past block cb: Ls and the partials are free
+                if (has_next && c0 == 0) nbar_arrive(8 + cb, kPipeThreads); // block 0's range, passed last
+                if (tid < kTP) {
+#pragma unroll
+                    for (int g = 0; g < 16; g++) {
+                        totS += partS[g * kTP + tid];
+                        totP += partP[g * kTP + tid];
+                    }
+                }
+                // partS / partP are rewritten only after the next block's
+                // first barrier
+            }
+            if (tid < kTP) {
+                const long long p = p0 + tid;
+                if (p < a.n_paths) {
+                    crash += (totS >= a.k) ? 1 : 0;
+                    breach += (a.has_w && totP < a.port_thr) ? 1 : 0;
+                    if (a.s_values) a.s_values[p] = totS;
+                    if (a.port_values) a.port_values[p] = totP;
+                    if (VAR) var_path(a, totP, shist, n_tail, tail_fx);
+                }
+            }
+        }
+    }
+    cta_flush(a, crash, breach, n_tail, tail_fx, sacc, VAR ? shist : nullptr, VAR);
+}
+
 int tiled_max_n() { return 768; }
 
 size_t tiled_smem_bytes(int n, int kt, int threads)
@@ -509,8 +740,9 @@ int tiled_npad(int n) { return (n + kWsTN - 1) / kWsTN * kWsTN; }
 // K padded to 16: a 16-row L^T slice never reads past the last row
 int tiled_kpad(int n) { return (n + 15) / 16 * 16; }
 
-// The phase-serial kernel unless RG_PLAIN_KERNEL names "ws" (the
-// warp-specialised kernel, kept for comparison: it measured slower).
+// The pipelined kernel unless RG_PLAIN_KERNEL names "serial" (the
+// phase-serial kernel) or "ws" (the warp-specialised kernel), both kept for
+// comparison.
 cudaError_t launch_tiled(const PlainArgs &a, const float *Lt, bool aggregated, int sm_count,
                          cudaStream_t s)
 {
@@ -525,6 +757,27 @@ cudaError_t launch_tiled(const PlainArgs &a, const float *Lt, bool aggregated, i
     t.sqrt_h = sqrtf((float)a.horizon);
     const char *env = getenv("RG_PLAIN_KERNEL");
     const bool ws = env && strstr(env, "ws") != nullptr;
+    const bool serial = env && strstr(env, "serial") != nullptr;
+    if (!ws && !serial) {
+        int dev = 0, optin = 0;
+        cudaError_t e = cudaGetDevice(&dev);
+        if (e == cudaSuccess) e = cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
+        if (e != cudaSuccess) return e;
+        const bool var = a.var_mode != 0;
+        const size_t static_bytes = 1024 + (var ? 4 * (size_t)(kVarHistBins + 2) : 0);
+        const bool kt16 = tiled_smem_bytes(a.n, 16, kTiledThreads) + static_bytes <= (size_t)optin;
+        const size_t smem = tiled_smem_bytes(a.n, kt16 ? 16 : 8, kTiledThreads);
+        void (*kern)(const TiledArgs) =
+            var ? (kt16 ? mc_tiled_pipe_kernel<true, 16> : mc_tiled_pipe_kernel<true, 8>)
+                : (kt16 ? mc_tiled_pipe_kernel<false, 16> : mc_tiled_pipe_kernel<false, 8>);
+        e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        if (e != cudaSuccess) return e;
+        long long tiles = (a.n_paths + kTP - 1) / kTP;
+        long long grid = sm_count;
+        if (tiles < grid) grid = tiles;
+        kern<<<(unsigned)grid, kPipeThreads, smem, s>>>(t);
+        return cudaGetLastError();
+    }
     if (ws) {
         const size_t smem = tiled_ws_smem_bytes(a.n);
         auto kern = (a.var_mode != 0) ? mc_tiled_ws_kernel<true> : mc_tiled_ws_kernel<false>;
