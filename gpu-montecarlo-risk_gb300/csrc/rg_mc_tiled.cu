@@ -41,7 +41,7 @@ static constexpr int kTiledThreads = 256;
 struct TiledArgs {
     PlainArgs a;          // counters, thresholds, Philox keys, VaR fields
     const float *Lt;      // [kpad][npad] L^T, FP32, zero padded
-    int kpad;             // N rounded up to 16 (tiled_kpad)
+    int kpad;             // N rounded up to 32 (tiled_kpad)
     int npad;             // N rounded up to 256 (a multiple of both column-block widths)
     int aggregated;       // 1: one N(0, H) draw per asset (sqrt(H) z)
     float sqrt_h;
@@ -737,8 +737,9 @@ size_t tiled_ws_smem_bytes(int n)
 
 // npad is a multiple of both column-block widths (128 and 256)
 int tiled_npad(int n) { return (n + kWsTN - 1) / kWsTN * kWsTN; }
-// K padded to 16: a 16-row L^T slice never reads past the last row
-int tiled_kpad(int n) { return (n + 15) / 16 * 16; }
+// K padded to 32: an L^T slice (up to 32 rows) never reads past the last
+// row, and a descending K loop ends exactly at row 0
+int tiled_kpad(int n) { return (n + 31) / 32 * 32; }
 
 // The pipelined kernel unless RG_PLAIN_KERNEL names "serial" (the
 // phase-serial kernel) or "ws" (the warp-specialised kernel), both kept for
@@ -765,11 +766,16 @@ cudaError_t launch_tiled(const PlainArgs &a, const float *Lt, bool aggregated, i
         if (e != cudaSuccess) return e;
         const bool var = a.var_mode != 0;
         const size_t static_bytes = 1024 + (var ? 4 * (size_t)(kVarHistBins + 2) : 0);
-        const bool kt16 = tiled_smem_bytes(a.n, 16, kTiledThreads) + static_bytes <= (size_t)optin;
-        const size_t smem = tiled_smem_bytes(a.n, kt16 ? 16 : 8, kTiledThreads);
+        // the widest L^T slice (32, 16 or 8 rows) whose shared memory fits
+        const int kt = tiled_smem_bytes(a.n, 32, kTiledThreads) + static_bytes <= (size_t)optin   ? 32
+                       : tiled_smem_bytes(a.n, 16, kTiledThreads) + static_bytes <= (size_t)optin ? 16
+                                                                                                  : 8;
+        const size_t smem = tiled_smem_bytes(a.n, kt, kTiledThreads);
         void (*kern)(const TiledArgs) =
-            var ? (kt16 ? mc_tiled_pipe_kernel<true, 16> : mc_tiled_pipe_kernel<true, 8>)
-                : (kt16 ? mc_tiled_pipe_kernel<false, 16> : mc_tiled_pipe_kernel<false, 8>);
+            var ? (kt == 32 ? mc_tiled_pipe_kernel<true, 32>
+                            : kt == 16 ? mc_tiled_pipe_kernel<true, 16> : mc_tiled_pipe_kernel<true, 8>)
+                : (kt == 32 ? mc_tiled_pipe_kernel<false, 32>
+                            : kt == 16 ? mc_tiled_pipe_kernel<false, 16> : mc_tiled_pipe_kernel<false, 8>);
         e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
         if (e != cudaSuccess) return e;
         long long tiles = (a.n_paths + kTP - 1) / kTP;
