@@ -722,7 +722,7 @@ def engine_arm(args):
         t_ideal = (flops_per_path / (peaks["fp32_tflops"] * 1e12)
                    + normals_drawn / peaks["normals_per_s"]) * count
         roofline = {"bound": "alu",
-                    "kernel": "rg::mc_rows_kernel<13,true,false>" if n <= 64 else "rg::mc_tiled_pipe_kernel<false,16>",
+                    "kernel": "rg::mc_rows_kernel<13,true,false>" if n <= 64 else "rg::mc_tiled_pipe_kernel<false,32>",
                     "achieved": tflops, "peak": peaks["fp32_tflops"], "unit": "TFLOP/s",
                     "frac": tflops / peaks["fp32_tflops"],
                     "peak_source": "measured live: FP32 FMA micro-kernel (rg_probe_peaks)",
@@ -734,7 +734,7 @@ def engine_arm(args):
         f = forms["fp32"]
         t_ideal = (flops_per_path / (peaks["fp32_tflops"] * 1e12)
                    + normals_drawn / peaks["normals_per_s"]) * count
-        f["roofline"] = {"kernel": "rg::mc_tiled_pipe_kernel<false,16>",
+        f["roofline"] = {"kernel": "rg::mc_tiled_pipe_kernel<false,32>",
                          "frac": flops_per_path * count / (f["ms_per_step"] * 1e-3) / (peaks["fp32_tflops"] * 1e12),
                          "composite_frac": t_ideal / (f["ms_per_step"] * 1e-3)}
 
