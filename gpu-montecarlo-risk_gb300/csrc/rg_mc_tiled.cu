@@ -4,7 +4,7 @@
 // at its definition: the pipelined mc_tiled_pipe_kernel (default), the
 // phase-serial mc_tiled_kernel it is built from (RG_PLAIN_KERNEL=serial) and
 // the warp-specialised mc_tiled_ws_kernel (RG_PLAIN_KERNEL=ws).  At N = 600,
-// H = 10, 1e7 paths: 124.5, 136.6 and 170 ms with daily draws; 94.0, 94.1
+// H = 10, 1e7 paths: 116.8, 136.6 and 170 ms with daily draws; 86.5, 94.1
 // and 149 ms with aggregated draws.
 //
 // Phase-serial form: a CTA owns a tile of 64 paths at a time (grid-stride
@@ -12,21 +12,23 @@
 //  1. Normals.  The 256 threads draw the tile's normals (Philox4x32-10 in
 //     the engine layout, Box-Muller, summed over the H days -- or one
 //     N(0, H) draw per asset in the aggregated mode) into shared memory,
-//     Zs[k][p] (asset-major rows of 64 paths, FP32).
+//     Zs[k][p] (asset-major rows of 64 paths, FP32), two quads per thread
+//     at a time with their Philox rounds interleaved.
 //  2. Contraction R = H mu + L Z as an FP32 GEMM over 128-asset column
 //     blocks: each thread holds a 4-path x 8-asset register tile, reads
 //     Z (float4, 4 paths) and L^T (two float4, 8 assets) from shared memory
-//     and accumulates with packed __ffma2_rn; the K loop of column block c
-//     stops at 128 (c+1) because L is lower triangular.  L^T slices (8 x 128)
-//     are staged by the CTA, double buffered with cp.async.
+//     and accumulates with packed __ffma2_rn.  L is lower triangular, so
+//     warp w (assets c0 + 16w .. c0 + 16w + 15) stops its multiply-adds at
+//     c0 + 16(w + 1).  L^T slices (KT x 128, KT = 16 where shared memory
+//     allows, else 8) are staged by the CTA, double buffered with cp.async.
 //  3. Per column block each thread folds its 4 x 8 returns into per-path
 //     partial crash counts and w.R partial sums in shared memory; the 16
 //     asset groups are summed in a fixed order (deterministic), and after
 //     the last block one thread per path forms S, w.R, the crash and breach
 //     flags and the VaR bookkeeping.
-// Shared memory: 4 * 64 * Kpad bytes for Z (155 KB at N = 600) + 8 KB of L
-// staging + 8 KB of partials (+ 16 KB of VaR histogram): one CTA per SM,
-// N <= 768.  Generation and the GEMM take turns on 8 warps per SM.
+// Shared memory: 256 x Kpad bytes for Z (156 KB at N = 600) + 2 x KT x 512
+// bytes of L staging + 8 KB of partials (+ 16 KB of VaR histogram): one CTA
+// per SM, N <= 768.  Generation and the GEMM take turns on 8 warps per SM.
 #include <cstdlib>
 #include <cstring>
 #include "rg_fused_kernel.cuh"
@@ -509,8 +511,9 @@ __global__ void __launch_bounds__(kWsThreadsT, 1) mc_tiled_ws_kernel(const Tiled
 // At N = 600 the bottom range, released last, is needed only at the end of
 // the next tile's top block, so generation and GEMM overlap almost entirely.
 // The GEMM is the phase-serial kernel's (4-path x 8-asset FFMA2 tiles,
-// 16-row L^T slices staged by cp.async, per-warp triangle cut) with a
-// barrier among the GEMM warps only.  Each return is the same terms as in
+// L^T slices of KT = 32 rows where shared memory allows, else 16 or 8,
+// staged by cp.async, per-warp triangle cut) with a barrier among the GEMM
+// warps only.  Each return is the same terms as in
 // the other forms, accumulated in descending k.
 // Named barriers, pairing by construction (both roles walk the same static
 // tile list and block count): 1 = GEMM warps (256); 2 + r = FILLED[r] (256
