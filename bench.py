@@ -26,8 +26,9 @@ Default workload (the configuration the headline metric is quoted on):
               tests/golden/oracle_figures.json; its input checksum is
               checked.
 `e2e`         the same metric through the public C ABI with host buffers
-              (rg_run: mu, Sigma and weights uploaded, factored on the GPU,
-              tensor tiles built, kernel run, counts read back) every step.
+              (rg_run: mu, Sigma and weights uploaded from pinned host
+              memory, factored on the GPU, tensor tiles built, kernel run,
+              counts read back) every step.
 `served`      Poisson arrivals at 2,000 queries/s of 1e5-path queries over
               64 resident portfolios through the server (continuous
               batching): p50/p99 latency and paths/s, against per-query
@@ -414,6 +415,14 @@ def se_units(r, fig, M):
 
 
 # ------------------------------------------------------------------ timing
+def pinned(a):
+    """A numpy view of a page-locked copy of `a` (the end-to-end legs upload
+    their inputs from pinned host memory)."""
+    import numpy as np
+    import torch
+    return torch.from_numpy(np.ascontiguousarray(a, dtype=np.float64)).pin_memory().numpy()
+
+
 def time_steps(port, q, counts, stream, flush, steps, warmup):
     """W untimed launches, then K launches each bracketed by CUDA events on
     the launching stream, L2 flushed before each outside the events.
@@ -598,7 +607,7 @@ def one_factor_50_measure(steps, warmup, flush, peaks):
     # end to end through the reference-facing plugin call (host mu, Sigma;
     # upload, factorisation, kernel and counts every call: cache off)
     os.environ["RG_PLUGIN_CACHE"] = "0"
-    call = riskgpu.PluginCall(p.mu, p.sigma)
+    call = riskgpu.PluginCall(pinned(p.mu), pinned(p.sigma))
     with quiet_stdout():
         call.run(M, p.k, p.x, p.seed)
         t0 = time.perf_counter()
@@ -798,13 +807,14 @@ def engine_arm(args):
         os.environ.pop("RG_RNG", None)
         if args.workload == "one_factor_50":
             os.environ["RG_PLUGIN_CACHE"] = "0"
-            call = riskgpu.PluginCall(p.mu, p.sigma)
+            call = riskgpu.PluginCall(pinned(p.mu), pinned(p.sigma))
             run_once = lambda: call.run(count, p.k, p.x, p.seed)["status"] == 0 or sys.exit("plugin call failed")
             e2e_path = "get_cuda_model().run_model (host mu/Sigma: upload, GPU Cholesky, kernel, counts back)"
             h2d = 8 * n + 8 * n * n
         else:
             qh = q_of(prec)
-            run_once = lambda: riskgpu.run(p.mu, p.sigma, p.weights, qh)
+            mu_h, sigma_h, w_h = pinned(p.mu), pinned(p.sigma), pinned(p.weights)
+            run_once = lambda: riskgpu.run(mu_h, sigma_h, w_h, qh)
             e2e_path = "rg_run (host mu/Sigma/weights: upload, GPU Cholesky, tiles, kernel, counts back)"
             h2d = 8 * n + 8 * n * n + 8 * n
         with quiet_stdout():
