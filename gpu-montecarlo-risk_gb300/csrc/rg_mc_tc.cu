@@ -294,18 +294,46 @@ __device__ __forceinline__ void tc_quad_sum2(int q, uint32_t plo, uint32_t phi, 
     }
 }
 
-__device__ __forceinline__ void split2(float v, int bf16, unsigned short &hi, unsigned short &lo)
+// Two FP32 values rounded to nearest and packed: a in bits 0-15, b in 16-31
+// (cvt's first source goes to the upper half).
+__device__ __forceinline__ uint32_t pack_bf16x2(float a, float b)
 {
-    if (bf16) {
-        const __nv_bfloat16 h = __float2bfloat16_rn(v);
-        const __nv_bfloat16 l = __float2bfloat16_rn(v - __bfloat162float(h));
-        hi = __bfloat16_as_ushort(h);
-        lo = __bfloat16_as_ushort(l);
+    uint32_t d;
+    asm("cvt.rn.bf16x2.f32 %0, %1, %2;" : "=r"(d) : "f"(b), "f"(a));
+    return d;
+}
+__device__ __forceinline__ uint32_t pack_f16x2(float a, float b)
+{
+    uint32_t d;
+    asm("cvt.rn.f16x2.f32 %0, %1, %2;" : "=r"(d) : "f"(b), "f"(a));
+    return d;
+}
+__device__ __forceinline__ float2 unpack_f16x2(uint32_t d)
+{
+    float2 r;
+    asm("{\n\t.reg .b16 l, h;\n\tmov.b32 {l, h}, %2;\n\tcvt.f32.f16 %0, l;\n\tcvt.f32.f16 %1, h;\n\t}"
+        : "=f"(r.x), "=f"(r.y)
+        : "r"(d));
+    return r;
+}
+
+// Hi/lo split of four FP32 values in the packed operand layout (element e
+// in bits 16 (e & 1) of word e >> 1): hi = round(v), lo = round(v - hi),
+// both round-to-nearest in BF16 or FP16.  A BF16 value widens to FP32 by a
+// 16-bit shift, so the BF16 form needs no conversion back.
+template <bool BF16>
+__device__ __forceinline__ void split4(const float4 v, uint2 &hi, uint2 &lo)
+{
+    if (BF16) {
+        const uint32_t a = pack_bf16x2(v.x, v.y), b = pack_bf16x2(v.z, v.w);
+        hi = make_uint2(a, b);
+        lo = make_uint2(pack_bf16x2(v.x - __uint_as_float(a << 16), v.y - __uint_as_float(a & 0xffff0000u)),
+                        pack_bf16x2(v.z - __uint_as_float(b << 16), v.w - __uint_as_float(b & 0xffff0000u)));
     } else {
-        const __half h = __float2half_rn(v);
-        const __half l = __float2half_rn(v - __half2float(h));
-        hi = __half_as_ushort(h);
-        lo = __half_as_ushort(l);
+        const uint32_t a = pack_f16x2(v.x, v.y), b = pack_f16x2(v.z, v.w);
+        const float2 fa = unpack_f16x2(a), fb = unpack_f16x2(b);
+        hi = make_uint2(a, b);
+        lo = make_uint2(pack_f16x2(v.x - fa.x, v.y - fa.y), pack_f16x2(v.z - fb.x, v.w - fb.y));
     }
 }
 
@@ -416,12 +444,12 @@ __global__ void __launch_bounds__(kTcThreads, 1) mc_tc_kernel(const __grid_const
                         if (it.aggregated)
                             for (int e = 0; e < 4; e++) z[e] *= it.sqrt_h;
                     }
-                    unsigned short h[4], l[4];
-                    for (int e = 0; e < 4; e++) split2(z[e], it.bf16, h[e], l[e]);
+                    uint2 hv, lv;
+                    const float4 zv = make_float4(z[0], z[1], z[2], z[3]);
+                    if (it.bf16) split4<true>(zv, hv, lv);
+                    else split4<false>(zv, hv, lv);
                     const int k = 4 * q, kt = k / kTcKt, kk = k % kTcKt;
                     const uint32_t off = (uint32_t)kt * kTcZBytes + sw128_offset(p, kk);
-                    const uint2 hv = make_uint2((uint32_t)h[0] | ((uint32_t)h[1] << 16), (uint32_t)h[2] | ((uint32_t)h[3] << 16));
-                    const uint2 lv = make_uint2((uint32_t)l[0] | ((uint32_t)l[1] << 16), (uint32_t)l[2] | ((uint32_t)l[3] << 16));
                     *reinterpret_cast<uint2 *>(zhi + off) = hv;
                     *reinterpret_cast<uint2 *>(zlo + off) = lv;
                 }
@@ -847,14 +875,12 @@ __global__ void __launch_bounds__(kWsThreads, 1) mc_tcws_kernel(const __grid_con
                     }
                     for (int u = 0; u < (two ? 2 : 1); u++) {
                         const float4 v = u ? y : z;
-                        const float zz[4] = {v.x, v.y, v.z, v.w};
-                        unsigned short h[4], l[4];
-                        for (int e = 0; e < 4; e++) split2(zz[e], it.bf16, h[e], l[e]);
+                        uint2 hv, lv;
+                        if (it.bf16) split4<true>(v, hv, lv);
+                        else split4<false>(v, hv, lv);
                         const uint32_t off = (uint32_t)zs * kZB + sw128_offset(u ? p2 : p, 4 * (u ? ql2 : ql));
-                        *reinterpret_cast<uint2 *>(zhi + off) =
-                            make_uint2((uint32_t)h[0] | ((uint32_t)h[1] << 16), (uint32_t)h[2] | ((uint32_t)h[3] << 16));
-                        *reinterpret_cast<uint2 *>(zlo + off) =
-                            make_uint2((uint32_t)l[0] | ((uint32_t)l[1] << 16), (uint32_t)l[2] | ((uint32_t)l[3] << 16));
+                        *reinterpret_cast<uint2 *>(zhi + off) = hv;
+                        *reinterpret_cast<uint2 *>(zlo + off) = lv;
                     }
                 }
                 fence_async_shared(); // this thread's writes -> async proxy (tensor cores)
