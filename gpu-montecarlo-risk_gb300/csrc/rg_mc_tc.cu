@@ -251,8 +251,9 @@ __host__ __device__ __forceinline__ uint32_t sw128_offset(int r, int k)
 }
 
 // Normals of quad q of one path summed over `days` draws (Philox counter
-// (d * nq + q, 0, path lo, path hi)); the paired form draws two quads of
-// two paths with their Philox rounds interleaved and gives the same sums.
+// (d * nq + q, 0, path lo, path hi)); the paired form draws two quads
+// (of one path or two) with their Philox rounds interleaved and gives the
+// same sums.
 __device__ __forceinline__ float4 tc_quad_sum(int q, int nq, int days, uint32_t plo, uint32_t phi,
                                               const PhiloxKeys &keys)
 {
@@ -626,7 +627,8 @@ __global__ void __launch_bounds__(kTcThreads, 1) mc_tc_kernel(const __grid_const
 //   warp 5       SPLIT: lane 0 streams the Lhat tiles (used when the MMAs
 //                bound the kernel, so refills never wait for the MMA thread)
 //   warps 5|6-31 (864 | 832 threads) generator: draws the normals one
-//                64-column K tile at a time into a ring of K-tile slots.
+//                64-column K tile at a time into a ring of K-tile slots, a
+//                thread drawing one path's two adjacent quads at a time.
 // The MMAs run K-tile-outer (for each K tile, every row tile that needs it),
 // so a K tile is needed only while its MMAs run: K tiles are numbered in
 // order across the CTA's path tiles (g), K tile g lives in slot g % kZSlots
@@ -840,29 +842,22 @@ __global__ void __launch_bounds__(kWsThreads, 1) mc_tcws_kernel(const __grid_con
                     atomicOr(b.err, 16u);
                     gab = 1;
                 }
-                const int per_kt = P * (kTcKt / 4);
-                // items of this thread in kt: global item index i = kt*per_kt + local,
-                // assigned round robin over the whole tile (i % kWsGenThreads == gtid)
+                // an item is one path's pair of adjacent quads (8 K columns,
+                // one 16-byte chunk of the swizzled Z row); items of kt are
+                // i = kt*per_kt + local, assigned round robin over the whole
+                // tile (i % kWsGenThreads == gtid)
+                const int per_kt = P * (kTcKt / 8);
                 int first = gtid - (kt * per_kt) % kWsGenThreads;
                 if (first < 0) first += kWsGenThreads;
-                // two items at a time (item, item + kWsGenThreads), their
-                // Philox rounds interleaved when both are real quads
                 const int days = it.aggregated ? 1 : it.horizon;
-                for (int item = first; item < per_kt; item += 2 * kWsGenThreads) {
-                    const int item2 = item + kWsGenThreads;
-                    const bool two = item2 < per_kt;
-                    const int ql = item / P, p = item - ql * P, q = kt * (kTcKt / 4) + ql;
-                    const int ql2 = two ? item2 / P : ql, p2 = two ? item2 - ql2 * P : p;
-                    const int q2 = kt * (kTcKt / 4) + ql2;
+                for (int item = first; item < per_kt; item += kWsGenThreads) {
+                    const int qp = item / P, p = item - qp * P, q = kt * (kTcKt / 4) + 2 * qp;
                     const unsigned long long path = it.path0 + (unsigned long long)(p0 + p);
-                    const unsigned long long path2 = it.path0 + (unsigned long long)(p0 + p2);
                     const uint32_t plo = (uint32_t)path, phi = (uint32_t)(path >> 32);
-                    const uint32_t plo2 = (uint32_t)path2, phi2 = (uint32_t)(path2 >> 32);
-                    const bool real1 = q < nq, real2 = two && q2 < nq;
+                    // the two quads' Philox rounds interleaved when both are real
                     float4 z = make_float4(0.f, 0.f, 0.f, 0.f), y = make_float4(0.f, 0.f, 0.f, 0.f);
-                    if (real1 && real2) tc_quad_sum2(q, plo, phi, q2, plo2, phi2, nq, days, it.keys, z, y);
-                    else if (real1) z = tc_quad_sum(q, nq, days, plo, phi, it.keys);
-                    else if (real2) y = tc_quad_sum(q2, nq, days, plo2, phi2, it.keys);
+                    if (q + 1 < nq) tc_quad_sum2(q, plo, phi, q + 1, plo, phi, nq, days, it.keys, z, y);
+                    else if (q < nq) z = tc_quad_sum(q, nq, days, plo, phi, it.keys);
                     if (it.aggregated) {
                         z.x *= it.sqrt_h;
                         z.y *= it.sqrt_h;
@@ -873,15 +868,18 @@ __global__ void __launch_bounds__(kWsThreads, 1) mc_tcws_kernel(const __grid_con
                         y.z *= it.sqrt_h;
                         y.w *= it.sqrt_h;
                     }
-                    for (int u = 0; u < (two ? 2 : 1); u++) {
-                        const float4 v = u ? y : z;
-                        uint2 hv, lv;
-                        if (it.bf16) split4<true>(v, hv, lv);
-                        else split4<false>(v, hv, lv);
-                        const uint32_t off = (uint32_t)zs * kZB + sw128_offset(u ? p2 : p, 4 * (u ? ql2 : ql));
-                        *reinterpret_cast<uint2 *>(zhi + off) = hv;
-                        *reinterpret_cast<uint2 *>(zlo + off) = lv;
+                    uint2 hz, lz, hy, ly;
+                    if (it.bf16) {
+                        split4<true>(z, hz, lz);
+                        split4<true>(y, hy, ly);
+                    } else {
+                        split4<false>(z, hz, lz);
+                        split4<false>(y, hy, ly);
                     }
+                    // padding quads (q >= nq) store zeros
+                    const uint32_t off = (uint32_t)zs * kZB + sw128_offset(p, 8 * qp);
+                    *reinterpret_cast<uint4 *>(zhi + off) = make_uint4(hz.x, hz.y, hy.x, hy.y);
+                    *reinterpret_cast<uint4 *>(zlo + off) = make_uint4(lz.x, lz.y, ly.x, ly.y);
                 }
                 fence_async_shared(); // this thread's writes -> async proxy (tensor cores)
                 mbar_arrive(&zfull[zs]);
