@@ -51,6 +51,7 @@ cores, on a bounded sample of the same workload.
 """
 import argparse
 import contextlib
+import dataclasses
 import hashlib
 import json
 import math
@@ -78,10 +79,10 @@ NCU_TRAFFIC_BYTES = {"one_factor_50": 42_496, "five_factor_600": 1_000_000}
 
 # Thread instructions the tcgen05 kernel issues per normal it draws, daily
 # draws at N = 600, H = 10 (ncu smsp__inst_executed.sum of a 1e6-path launch,
-# 3.996e9 warp instructions x 32 / 6e9 normals).  With the SM count and the
+# 3.716e9 warp instructions x 32 / 6e9 normals).  With the SM count and the
 # sampled SM clock it gives the kernel's issue bound: every SM issuing 4 warp
 # instructions (128 thread instructions) a cycle.
-TC_THREAD_INST_PER_NORMAL = 21.3
+TC_THREAD_INST_PER_NORMAL = 19.8
 
 
 def parse():
@@ -101,6 +102,9 @@ def parse():
                     choices=["five_factor_600", "one_factor_50", "batch_256", "served"],
                     help="five_factor_600 (N=600, H=10, 1e7 paths per step) is the headline; "
                          "one_factor_50 is the drop-in workload alone")
+    ap.add_argument("--horizon", type=int, default=None,
+                    help="override five_factor_600's 10-day horizon (instruction-count sweeps over the "
+                         "horizon; the headline uses the workload's own)")
     ap.add_argument("--draw-mode", default="daily", choices=["daily", "aggregated"])
     ap.add_argument("--precision", default="auto", choices=["auto", "fp32", "bf16x3", "fp16x3"],
                     help="auto: bf16x3 for five_factor_600, fp32 for one_factor_50")
@@ -123,7 +127,12 @@ def workload(args):
         return synth.one_factor_50(n_paths=args.paths)
     if args.paths is None:
         args.paths = 10_000_000
-    return synth.five_factor_600(n_paths=args.paths)
+    p = synth.five_factor_600(n_paths=args.paths)
+    if args.horizon is not None:
+        if args.horizon < 1:
+            raise SystemExit("--horizon must be >= 1")
+        p = dataclasses.replace(p, horizon=args.horizon)
+    return p
 
 
 def precision_name(args):

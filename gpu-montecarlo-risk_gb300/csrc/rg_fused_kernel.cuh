@@ -17,9 +17,11 @@
 //    H mu_i + sum.x + sum.y.  Rows of group g are final at once: compared
 //    with -x and folded into S and w.R.
 //  * L (packed lower rows), H*mu and w live in the kernel's parameter space,
-//    indexed with compile-time offsets, so every FMA takes its L pair as a
-//    constant-bank operand: no shared-memory or global loads in the loop.
-//    The parameter block is at most 64 packed rows (8.7 KB) plus 2 x 256 B.
+//    indexed with compile-time offsets: no shared-memory or global loads in
+//    the loop.  The packed FFMA2 takes its L pair from registers, so the
+//    pairs come through the constant cache (instruction counts: about one
+//    load per two FFMA2).  The parameter block is at most 64 packed rows
+//    (8.7 KB) plus 2 x 256 B.
 //  * Counts: per-thread integers -> warp reduction -> one 64-bit atomic per
 //    CTA per counter.
 #pragma once
