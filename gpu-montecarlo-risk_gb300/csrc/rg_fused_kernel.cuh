@@ -39,7 +39,8 @@ struct ConstBlock {
     float4 w[NQ];                     // weights (zeros when none)
 };
 
-// Normals of quad q of one path, summed over the horizon.
+// Normals of quad q of one path, summed over the horizon, divided by
+// sqrt(2 ln 2) (the launcher folds that factor into L).
 // `second` = false skips the second Box-Muller pair (the last quad when
 // N mod 4 is 1 or 2: those normals feed only padding rows).
 template <int NQ, bool ONE_DAY>
@@ -49,15 +50,15 @@ __device__ __forceinline__ float4 fused_quad_normals(int q, int horizon, uint32_
     float4 z = make_float4(0.f, 0.f, 0.f, 0.f);
     {
         const uint4 w = rg_philox(make_uint4((uint32_t)q, 0u, plo, phi), keys);
-        rg_box_muller(w.x, w.y, z.x, z.y);
-        if (second) rg_box_muller(w.z, w.w, z.z, z.w);
+        rg_box_muller_unscaled(w.x, w.y, z.x, z.y);
+        if (second) rg_box_muller_unscaled(w.z, w.w, z.z, z.w);
     }
     if (!ONE_DAY) {
         for (int d = 1; d < horizon; d++) {
             const uint4 w = rg_philox(make_uint4((uint32_t)(d * NQ + q), 0u, plo, phi), keys);
             float z0, z1, z2 = 0.f, z3 = 0.f;
-            rg_box_muller(w.x, w.y, z0, z1);
-            if (second) rg_box_muller(w.z, w.w, z2, z3);
+            rg_box_muller_unscaled(w.x, w.y, z0, z1);
+            if (second) rg_box_muller_unscaled(w.z, w.w, z2, z3);
             z.x += z0;
             z.y += z1;
             z.z += z2;
@@ -229,9 +230,10 @@ static cudaError_t launch_fused_nq(const PlainArgs &a, const float *Lp_host, con
     ConstBlock<NQ> cb;
     memset(&cb, 0, sizeof(cb));
     memcpy(cb.L, Lp_host, sizeof(float) * (size_t)packed_len(a.n));
-    if (a.aggregated) {
-        // one N(0,1) draw per asset: R = H mu + (sqrt(H) L) z
-        const float sh = sqrtf((float)a.horizon);
+    {
+        // the kernel draws z / sqrt(2 ln 2) (rg_box_muller_unscaled): R = H mu + (s L) z with
+        // s = sqrt(2 ln 2), times sqrt(H) with one N(0, 1) draw per asset (aggregated)
+        const float sh = (float)((double)kBmScale * (a.aggregated ? std::sqrt((double)a.horizon) : 1.0));
         float *Lf = reinterpret_cast<float *>(cb.L);
         for (int i = 0; i < packed_len(a.n); i++) Lf[i] *= sh;
     }

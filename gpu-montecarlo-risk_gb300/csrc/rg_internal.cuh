@@ -113,6 +113,22 @@ __device__ __forceinline__ void rg_box_muller(uint32_t a, uint32_t b, float &z0,
     z1 = r * rg_sin_approx(t);
 }
 
+// sqrt(2 ln 2): r = sqrt(-2 ln u) = kBmScale sqrt(-log2 u).
+static constexpr float kBmScale = 1.1774100225154747f;
+
+// Box-Muller as above without the factor sqrt(2 ln 2) of r: returns
+// (z0, z1) / sqrt(2 ln 2), one multiply fewer a pair.  For callers that sum
+// several draws and scale the sum once.
+__device__ __forceinline__ void rg_box_muller_unscaled(uint32_t a, uint32_t b, float &z0, float &z1)
+{
+    const float ua = 2.0f - rg_one_to_two(a);          // (0, 1]
+    const float v = rg_one_to_two(b) - 1.5f;           // [-1/2, 1/2)
+    const float r = rg_sqrt_approx(-rg_lg2_approx(ua));
+    const float t = 6.283185307179586f * v;
+    z0 = r * rg_cos_approx(t);
+    z1 = r * rg_sin_approx(t);
+}
+
 // Packed FP32 lower-triangular rows: row i holds L[i][0..i] zero-padded to
 // a multiple of 4 floats, so every row starts on a 16-byte boundary.
 // offset(i) = sum_{r<i} 4 ceil((r+1)/4) = 4 (a+1)(2a+b) for i = 4a+b.

@@ -69,7 +69,8 @@ struct TcItem {
     PhiloxKeys keys;
     double hwmu;                  // H w.mu
     int n, n_mt, n_kt, horizon, k, has_w, aggregated, bf16;
-    float neg_x, port_thr, sqrt_h, hwmu_f;  // hwmu_f = (float) hwmu
+    float neg_x, port_thr, hwmu_f;  // hwmu_f = (float) hwmu
+    float zscale;  // factor of each summed normal: sqrt(2 ln 2) (the draws are unscaled), x sqrt(H) aggregated
 };
 
 struct TcBatch {
@@ -251,7 +252,8 @@ __host__ __device__ __forceinline__ uint32_t sw128_offset(int r, int k)
 }
 
 // Normals of quad q of one path summed over `days` draws (Philox counter
-// (d * nq + q, 0, path lo, path hi)); the paired form draws two quads
+// (d * nq + q, 0, path lo, path hi)), divided by sqrt(2 ln 2): the caller
+// scales each sum once (TcItem::zscale).  The paired form draws two quads
 // (of one path or two) with their Philox rounds interleaved and gives the
 // same sums.
 __device__ __forceinline__ float4 tc_quad_sum(int q, int nq, int days, uint32_t plo, uint32_t phi,
@@ -261,8 +263,8 @@ __device__ __forceinline__ float4 tc_quad_sum(int q, int nq, int days, uint32_t 
     for (int d = 0; d < days; d++) {
         const uint4 wv = rg_philox(make_uint4((uint32_t)(d * nq + q), 0u, plo, phi), keys);
         float z0, z1, z2, z3;
-        rg_box_muller(wv.x, wv.y, z0, z1);
-        rg_box_muller(wv.z, wv.w, z2, z3);
+        rg_box_muller_unscaled(wv.x, wv.y, z0, z1);
+        rg_box_muller_unscaled(wv.z, wv.w, z2, z3);
         z.x += z0;
         z.y += z1;
         z.z += z2;
@@ -280,10 +282,10 @@ __device__ __forceinline__ void tc_quad_sum2(int q, uint32_t plo, uint32_t phi, 
         uint4 wb = make_uint4((uint32_t)(d * nq + q2), 0u, plo2, phi2);
         rg_philox2(wa, wb, keys);
         float z0, z1, z2, z3, y0, y1, y2, y3;
-        rg_box_muller(wa.x, wa.y, z0, z1);
-        rg_box_muller(wa.z, wa.w, z2, z3);
-        rg_box_muller(wb.x, wb.y, y0, y1);
-        rg_box_muller(wb.z, wb.w, y2, y3);
+        rg_box_muller_unscaled(wa.x, wa.y, z0, z1);
+        rg_box_muller_unscaled(wa.z, wa.w, z2, z3);
+        rg_box_muller_unscaled(wb.x, wb.y, y0, y1);
+        rg_box_muller_unscaled(wb.z, wb.w, y2, y3);
         z.x += z0;
         z.y += z1;
         z.z += z2;
@@ -435,15 +437,14 @@ __global__ void __launch_bounds__(kTcThreads, 1) mc_tc_kernel(const __grid_const
                         for (int d = 0; d < days; d++) {
                             const uint4 wv = rg_philox(make_uint4((uint32_t)(d * nq + q), 0u, plo, phi), it.keys);
                             float z0, z1, z2, z3;
-                            rg_box_muller(wv.x, wv.y, z0, z1);
-                            rg_box_muller(wv.z, wv.w, z2, z3);
+                            rg_box_muller_unscaled(wv.x, wv.y, z0, z1);
+                            rg_box_muller_unscaled(wv.z, wv.w, z2, z3);
                             z[0] += z0;
                             z[1] += z1;
                             z[2] += z2;
                             z[3] += z3;
                         }
-                        if (it.aggregated)
-                            for (int e = 0; e < 4; e++) z[e] *= it.sqrt_h;
+                        for (int e = 0; e < 4; e++) z[e] *= it.zscale;
                     }
                     uint2 hv, lv;
                     const float4 zv = make_float4(z[0], z[1], z[2], z[3]);
@@ -858,16 +859,14 @@ __global__ void __launch_bounds__(kWsThreads, 1) mc_tcws_kernel(const __grid_con
                     float4 z = make_float4(0.f, 0.f, 0.f, 0.f), y = make_float4(0.f, 0.f, 0.f, 0.f);
                     if (q + 1 < nq) tc_quad_sum2(q, plo, phi, q + 1, plo, phi, nq, days, it.keys, z, y);
                     else if (q < nq) z = tc_quad_sum(q, nq, days, plo, phi, it.keys);
-                    if (it.aggregated) {
-                        z.x *= it.sqrt_h;
-                        z.y *= it.sqrt_h;
-                        z.z *= it.sqrt_h;
-                        z.w *= it.sqrt_h;
-                        y.x *= it.sqrt_h;
-                        y.y *= it.sqrt_h;
-                        y.z *= it.sqrt_h;
-                        y.w *= it.sqrt_h;
-                    }
+                    z.x *= it.zscale;
+                    z.y *= it.zscale;
+                    z.z *= it.zscale;
+                    z.w *= it.zscale;
+                    y.x *= it.zscale;
+                    y.y *= it.zscale;
+                    y.z *= it.zscale;
+                    y.w *= it.zscale;
                     uint2 hz, lz, hy, ly;
                     if (it.bf16) {
                         split4<true>(z, hz, lz);
@@ -1258,7 +1257,7 @@ static void fill_item(TcItem &it, const PlainArgs &a, const unsigned char *tiles
     it.bf16 = bf16;
     it.neg_x = a.neg_x;
     it.port_thr = a.port_thr;
-    it.sqrt_h = sqrtf((float)a.horizon);
+    it.zscale = (float)((double)kBmScale * (aggregated ? std::sqrt((double)a.horizon) : 1.0));
 }
 
 template <class K>

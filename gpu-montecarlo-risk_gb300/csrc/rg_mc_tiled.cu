@@ -46,7 +46,7 @@ struct TiledArgs {
     int kpad;             // N rounded up to 32 (tiled_kpad)
     int npad;             // N rounded up to 256 (a multiple of both column-block widths)
     int aggregated;       // 1: one N(0, H) draw per asset (sqrt(H) z)
-    float sqrt_h;
+    float zscale;         // factor of each summed normal: sqrt(2 ln 2) (the draws are unscaled), x sqrt(H) aggregated
 };
 
 __device__ __forceinline__ void cp_async16(void *smem, const void *gmem)
@@ -112,10 +112,10 @@ __global__ void __launch_bounds__(THREADS, 1) mc_tiled_kernel(const TiledArgs t)
                     uint4 wb = make_uint4((uint32_t)(d * nq + q2), 0u, plo, phi);
                     rg_philox2(wa, wb, a.keys);
                     float z0, z1, z2, z3, y0, y1, y2, y3;
-                    rg_box_muller(wa.x, wa.y, z0, z1);
-                    rg_box_muller(wa.z, wa.w, z2, z3);
-                    rg_box_muller(wb.x, wb.y, y0, y1);
-                    rg_box_muller(wb.z, wb.w, y2, y3);
+                    rg_box_muller_unscaled(wa.x, wa.y, z0, z1);
+                    rg_box_muller_unscaled(wa.z, wa.w, z2, z3);
+                    rg_box_muller_unscaled(wb.x, wb.y, y0, y1);
+                    rg_box_muller_unscaled(wb.z, wb.w, y2, y3);
                     z.x += z0;
                     z.y += z1;
                     z.z += z2;
@@ -125,16 +125,14 @@ __global__ void __launch_bounds__(THREADS, 1) mc_tiled_kernel(const TiledArgs t)
                     y.z += y2;
                     y.w += y3;
                 }
-                if (t.aggregated) {
-                    z.x *= t.sqrt_h;
-                    z.y *= t.sqrt_h;
-                    z.z *= t.sqrt_h;
-                    z.w *= t.sqrt_h;
-                    y.x *= t.sqrt_h;
-                    y.y *= t.sqrt_h;
-                    y.z *= t.sqrt_h;
-                    y.w *= t.sqrt_h;
-                }
+                z.x *= t.zscale;
+                z.y *= t.zscale;
+                z.z *= t.zscale;
+                z.w *= t.zscale;
+                y.x *= t.zscale;
+                y.y *= t.zscale;
+                y.z *= t.zscale;
+                y.w *= t.zscale;
                 if (q >= nq) z = make_float4(0.f, 0.f, 0.f, 0.f); // padding rows
                 if (q2 >= nq) y = make_float4(0.f, 0.f, 0.f, 0.f);
                 Zs[(4 * q + 0) * kTP + p] = z.x;
@@ -354,19 +352,17 @@ __global__ void __launch_bounds__(kWsThreadsT, 1) mc_tiled_ws_kernel(const Tiled
                     for (int d = 0; d < days; d++) {
                         const uint4 wv = rg_philox(make_uint4((uint32_t)(d * nq + q), 0u, plo, phi), a.keys);
                         float z0, z1, z2, z3;
-                        rg_box_muller(wv.x, wv.y, z0, z1);
-                        rg_box_muller(wv.z, wv.w, z2, z3);
+                        rg_box_muller_unscaled(wv.x, wv.y, z0, z1);
+                        rg_box_muller_unscaled(wv.z, wv.w, z2, z3);
                         z.x += z0;
                         z.y += z1;
                         z.z += z2;
                         z.w += z3;
                     }
-                    if (t.aggregated) {
-                        z.x *= t.sqrt_h;
-                        z.y *= t.sqrt_h;
-                        z.z *= t.sqrt_h;
-                        z.w *= t.sqrt_h;
-                    }
+                    z.x *= t.zscale;
+                    z.y *= t.zscale;
+                    z.z *= t.zscale;
+                    z.w *= t.zscale;
                 }
                 Z[(4 * q + 0) * kWsP + p] = z.x;
                 Z[(4 * q + 1) * kWsP + p] = z.y;
@@ -570,10 +566,10 @@ __global__ void __launch_bounds__(kPipeThreads, 1) mc_tiled_pipe_kernel(const Ti
                         uint4 wb = make_uint4((uint32_t)(d * nq + q2), 0u, plo, phi);
                         rg_philox2(wa, wb, a.keys);
                         float z0, z1, z2, z3, y0, y1, y2, y3;
-                        rg_box_muller(wa.x, wa.y, z0, z1);
-                        rg_box_muller(wa.z, wa.w, z2, z3);
-                        rg_box_muller(wb.x, wb.y, y0, y1);
-                        rg_box_muller(wb.z, wb.w, y2, y3);
+                        rg_box_muller_unscaled(wa.x, wa.y, z0, z1);
+                        rg_box_muller_unscaled(wa.z, wa.w, z2, z3);
+                        rg_box_muller_unscaled(wb.x, wb.y, y0, y1);
+                        rg_box_muller_unscaled(wb.z, wb.w, y2, y3);
                         z.x += z0;
                         z.y += z1;
                         z.z += z2;
@@ -583,16 +579,14 @@ __global__ void __launch_bounds__(kPipeThreads, 1) mc_tiled_pipe_kernel(const Ti
                         y.z += y2;
                         y.w += y3;
                     }
-                    if (t.aggregated) {
-                        z.x *= t.sqrt_h;
-                        z.y *= t.sqrt_h;
-                        z.z *= t.sqrt_h;
-                        z.w *= t.sqrt_h;
-                        y.x *= t.sqrt_h;
-                        y.y *= t.sqrt_h;
-                        y.z *= t.sqrt_h;
-                        y.w *= t.sqrt_h;
-                    }
+                    z.x *= t.zscale;
+                    z.y *= t.zscale;
+                    z.z *= t.zscale;
+                    z.w *= t.zscale;
+                    y.x *= t.zscale;
+                    y.y *= t.zscale;
+                    y.z *= t.zscale;
+                    y.w *= t.zscale;
                     if (q >= nq) z = make_float4(0.f, 0.f, 0.f, 0.f); // padding rows
                     if (q2 >= nq) y = make_float4(0.f, 0.f, 0.f, 0.f);
                     Zs[(4 * q + 0) * kTP + p] = z.x;
@@ -758,7 +752,7 @@ cudaError_t launch_tiled(const PlainArgs &a, const float *Lt, bool aggregated, i
     t.kpad = tiled_kpad(a.n);
     t.npad = tiled_npad(a.n);
     t.aggregated = aggregated ? 1 : 0;
-    t.sqrt_h = sqrtf((float)a.horizon);
+    t.zscale = (float)((double)kBmScale * (aggregated ? std::sqrt((double)a.horizon) : 1.0));
     const char *env = getenv("RG_PLAIN_KERNEL");
     const bool ws = env && strstr(env, "ws") != nullptr;
     const bool serial = env && strstr(env, "serial") != nullptr;

@@ -41,10 +41,11 @@ __global__ void __launch_bounds__(kProbeThreads) probe_normals_kernel(int iters,
     for (int i = 0; i < iters; i++) {
         const uint4 r = rg_philox(make_uint4((uint32_t)i, 0u, path, 0u), keys);
         float z0, z1, z2, z3;
-        rg_box_muller(r.x, r.y, z0, z1);
-        rg_box_muller(r.z, r.w, z2, z3);
+        rg_box_muller_unscaled(r.x, r.y, z0, z1);
+        rg_box_muller_unscaled(r.z, r.w, z2, z3);
         acc += (z0 + z1) + (z2 + z3);
     }
+    acc *= kBmScale; // the kernels scale each summed normal once
     if (acc == -12345.f) sink[0] = acc;
 }
 
