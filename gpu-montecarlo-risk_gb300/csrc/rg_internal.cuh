@@ -8,8 +8,8 @@
 //   rg_box_muller   Box-Muller (Box & Muller 1958) on two 32-bit words.
 //                   The top 23 bits of a word w form f = 1 + (w >> 9) 2^-23 in
 //                   [1, 2) by setting the exponent bits (no int->float
-//                   conversion); u_a = 2 - f in (0, 1], v = f_b - 3/2 in
-//                   [-1/2, 1/2); r = sqrt(-2 ln u_a), t = 2 pi v,
+//                   conversion); u_a = 2 - f in (0, 1], t = 2 pi f_b in
+//                   [2 pi, 4 pi) (a uniform angle), r = sqrt(-2 ln u_a),
 //                   (z0, z1) = (r cos t, r sin t), using the hardware
 //                   approximate lg2/sqrt/sin/cos (PTX *.approx).  The
 //                   smallest u_a is 2^-23, so |z| <= sqrt(46 ln 2) = 5.65.
@@ -105,10 +105,9 @@ __device__ __forceinline__ float rg_one_to_two(uint32_t w)
 __device__ __forceinline__ void rg_box_muller(uint32_t a, uint32_t b, float &z0, float &z1)
 {
     const float ua = 2.0f - rg_one_to_two(a);          // (0, 1]
-    const float v = rg_one_to_two(b) - 1.5f;           // [-1/2, 1/2)
     // -2 ln(u) = -2 ln(2) log2(u)
     const float r = rg_sqrt_approx(-1.3862943611198906f * rg_lg2_approx(ua));
-    const float t = 6.283185307179586f * v;
+    const float t = 6.283185307179586f * rg_one_to_two(b); // [2 pi, 4 pi)
     z0 = r * rg_cos_approx(t);
     z1 = r * rg_sin_approx(t);
 }
@@ -122,9 +121,8 @@ static constexpr float kBmScale = 1.1774100225154747f;
 __device__ __forceinline__ void rg_box_muller_unscaled(uint32_t a, uint32_t b, float &z0, float &z1)
 {
     const float ua = 2.0f - rg_one_to_two(a);          // (0, 1]
-    const float v = rg_one_to_two(b) - 1.5f;           // [-1/2, 1/2)
     const float r = rg_sqrt_approx(-rg_lg2_approx(ua));
-    const float t = 6.283185307179586f * v;
+    const float t = 6.283185307179586f * rg_one_to_two(b); // [2 pi, 4 pi)
     z0 = r * rg_cos_approx(t);
     z1 = r * rg_sin_approx(t);
 }

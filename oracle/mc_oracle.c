@@ -238,14 +238,14 @@ void orc_philox4x32_10(const uint32_t ctr_in[4], const uint32_t key_in[2], uint3
 static inline double engine_one_to_two(uint32_t w) { return 1.0 + (double)(w >> 9) * 0x1p-23; }
 
 /* Box-Muller on one pair of 32-bit words, in FP64 from the engine's
- * uniforms u_a = 2 - f(a) in (0, 1], v = f(b) - 3/2 in [-1/2, 1/2):
- * z0 = r cos(t), z1 = r sin(t), r = sqrt(-2 ln u_a), t = 2 pi v. */
+ * uniforms u_a = 2 - f(a) in (0, 1] and angle t = 2 pi f(b) in [2 pi, 4 pi):
+ * z0 = r cos(t), z1 = r sin(t), r = sqrt(-2 ln u_a). */
 static inline void box_muller(uint32_t a, uint32_t b, double *z0, double *z1)
 {
     const double two_pi = 6.283185307179586476925286766559;
-    double ua = 2.0 - engine_one_to_two(a), v = engine_one_to_two(b) - 1.5;
+    double ua = 2.0 - engine_one_to_two(a);
     double r = sqrt(-2.0 * log(ua));
-    double t = two_pi * v;
+    double t = two_pi * engine_one_to_two(b);
     *z0 = r * cos(t);
     *z1 = r * sin(t);
 }
