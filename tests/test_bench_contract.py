@@ -27,3 +27,32 @@ def test_reference_arm_line():
     assert d["e2e"]["value"] == d["value"]
     assert d["sample_paths_per_step"] > 0 and d["ms_per_step_basis"].startswith("measured")
     assert d["ms_per_full_step_extrapolated"] > 0
+
+
+def test_horizon_override_changes_only_the_horizon():
+    """--horizon (instruction-count sweeps) replaces five_factor_600's 10-day
+    horizon and nothing else; values below one day are refused."""
+    sys.path.insert(0, ROOT)
+    sys.path.insert(0, os.path.join(ROOT, "gpu-montecarlo-risk_gb300"))
+    import importlib
+    bench = importlib.import_module("bench")
+    argv = sys.argv
+    try:
+        sys.argv = ["bench.py", "--paths", "1000"]
+        base = bench.workload(bench.parse())
+        sys.argv = ["bench.py", "--paths", "1000", "--horizon", "2"]
+        args = bench.parse()
+        p = bench.workload(args)
+        assert base.horizon == 10 and p.horizon == 2
+        assert p.n == base.n and p.k == base.k and p.x == base.x and p.seed == base.seed
+        assert (p.mu == base.mu).all() and (p.sigma == base.sigma).all()
+        assert bench.config(args, 1, p)["horizon_days"] == 2
+        sys.argv = ["bench.py", "--paths", "1000", "--horizon", "0"]
+        try:
+            bench.workload(bench.parse())
+        except SystemExit:
+            pass
+        else:
+            raise AssertionError("--horizon 0 was accepted")
+    finally:
+        sys.argv = argv
