@@ -53,6 +53,7 @@ static constexpr int kTcZBytes = kTcPaths * kTcKt * 2;    // one part of a Z K t
 static constexpr float kTcLScale = 256.0f;
 static constexpr unsigned kTcSpinLimit = 1u << 26;        // try_wait polls before giving up
 static constexpr unsigned long long kTcWaitNs = 2000000000ull; // 2 s of wall time
+static constexpr unsigned kTcSuspendNs = 1u << 16;           // try_wait suspend hint (65 us)
 
 // One (portfolio, query) of a launch.  Tiles of 64 paths are numbered
 // globally across the items of a launch; item i owns tiles
@@ -125,6 +126,20 @@ __device__ __forceinline__ bool mbar_try_wait(uint64_t *bar, unsigned parity)
                  : "memory");
     return ok != 0;
 }
+// The same with a suspend-time hint: a waiting thread sleeps until the phase
+// completes or about `ns` nanoseconds pass, instead of the hardware's
+// shorter default, so long waits cost few polls (issue slots).
+__device__ __forceinline__ bool mbar_try_wait_hint(uint64_t *bar, unsigned parity, unsigned ns)
+{
+    uint32_t ok;
+    asm volatile("{\n\t.reg .pred p;\n\t"
+                 "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2, %3;\n\t"
+                 "selp.u32 %0, 1, 0, p;\n\t}"
+                 : "=r"(ok)
+                 : "r"(smem_u32(bar)), "r"(parity), "r"(ns)
+                 : "memory");
+    return ok != 0;
+}
 // Non-blocking probe of a phase (mbarrier.test_wait never suspends).
 __device__ __forceinline__ bool mbar_test(uint64_t *bar, unsigned parity)
 {
@@ -150,8 +165,8 @@ __device__ __forceinline__ bool mbar_wait(uint64_t *bar, unsigned parity)
     if (mbar_try_wait(bar, parity)) return true; // common case: no timer read
     const unsigned long long t0 = global_ns();
     for (unsigned i = 0; i < kTcSpinLimit; i++) {
-        if (mbar_try_wait(bar, parity)) return true;
-        if ((i & 255u) == 255u && global_ns() - t0 > kTcWaitNs) return false;
+        if (mbar_try_wait_hint(bar, parity, kTcSuspendNs)) return true;
+        if ((i & 15u) == 15u && global_ns() - t0 > kTcWaitNs) return false;
     }
     return false;
 }
