@@ -84,3 +84,72 @@ def test_binary_layout_round_trip(tmp_path):
     assert len(open(os.path.join(tmp_path, "params.bin"), "rb").read()) == 8
     m2, s2, f2 = preprocess.load_results_binary(str(tmp_path))
     assert np.array_equal(m2, mu) and np.array_equal(s2, sigma) and f2 == 0.0123
+
+
+REFERENCE_TREE = "/root/reference"
+
+
+def _reference_config():
+    """The index files and parameters of the reference's config.yaml, read
+    as text (PyYAML is not assumed): indices, start, end, train_ratio, x, k."""
+    path = os.path.join(REFERENCE_TREE, "config.yaml")
+    indices, cfg, in_idx = {}, {}, False
+    for line in open(path):
+        text = line.split("#", 1)[0].rstrip()
+        if not text.strip():
+            continue
+        if not line.startswith(" "):
+            in_idx = text.startswith("indices:")
+            if ":" in text and not in_idx:
+                key, val = text.split(":", 1)
+                cfg[key.strip()] = val.strip().strip('"')
+            continue
+        if in_idx and ":" in text:
+            key, val = text.split(":", 1)
+            indices[key.strip()] = val.strip().strip('"')
+    return indices, cfg
+
+
+@pytest.mark.skipif(not os.path.isdir(os.path.join(REFERENCE_TREE, "dataset")),
+                    reason="the reference's index files are not on this machine")
+def test_reference_dataset_split_matches_the_oracle(oracle):
+    """The reference's own index files and config.yaml (15 indices, daily
+    returns since 2015, 80/20 split): the engine's reader, alignment and split
+    against the oracle's plain-Python restatement, row by row, and the
+    training moments and realised crash frequency against the oracle's."""
+    import csv
+    import math
+    indices, cfg = _reference_config()
+    assert len(indices) >= 5
+    dataset = os.path.join(REFERENCE_TREE, "dataset")
+    start, end = cfg["start"], cfg["end"]
+    ratio, x, k = float(cfg["train_ratio"]), float(cfg["x"]), int(cfg["k"])
+    train, test = preprocess.fetch_and_split(indices, dataset, start=start, end=end, train_ratio=ratio)
+
+    series = {}
+    for name, fname in indices.items():
+        rows = []
+        with open(os.path.join(dataset, fname), newline="") as f:
+            for row in csv.DictReader(f):
+                try:
+                    d = dt.datetime.strptime(row["Date"].strip(), "%m/%d/%Y").date()
+                except ValueError:
+                    continue
+                try:
+                    r = float(row["Return"])
+                except (TypeError, ValueError):
+                    r = None
+                rows.append((d, None if r is None or math.isnan(r) else r))
+        series[name] = rows
+    to_date = lambda s: dt.date.fromisoformat(s)
+    ref_train, ref_test = oracle.align_and_split(series, to_date(start), to_date(end), ratio)
+    for got, ref in ((train, ref_train), (test, ref_test)):
+        assert len(got) == len(ref) and len(got) > 100
+        assert [np.datetime64(d, "D") for d, _ in ref] == list(got.dates)
+        assert np.array_equal(np.array([v for _, v in ref], dtype=np.float64), got.values)
+    assert train.names == list(indices)
+    assert train.dates[-1] < test.dates[0]
+    mu, sigma = oracle.compute_stats(train.values)
+    assert mu.shape == (len(indices),) and np.all(np.linalg.eigvalsh(sigma) > 0)
+    freq = oracle.compute_metrics(test.values, x, k)
+    assert 0.0 <= freq <= 1.0
