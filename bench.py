@@ -121,6 +121,8 @@ def dist_env():
 def workload(args):
     """The synthetic portfolio of the workload, sized to the paths per step."""
     from riskgpu import synth
+    if args.horizon is not None and args.workload != "five_factor_600":
+        raise SystemExit("--horizon applies to the five_factor_600 workload only")
     if args.workload == "one_factor_50":
         if args.paths is None:
             args.paths = 100_000_000

@@ -54,5 +54,12 @@ def test_horizon_override_changes_only_the_horizon():
             pass
         else:
             raise AssertionError("--horizon 0 was accepted")
+        sys.argv = ["bench.py", "--workload", "one_factor_50", "--paths", "1000", "--horizon", "2"]
+        try:
+            bench.workload(bench.parse())
+        except SystemExit:
+            pass
+        else:
+            raise AssertionError("--horizon was accepted for one_factor_50")
     finally:
         sys.argv = argv
