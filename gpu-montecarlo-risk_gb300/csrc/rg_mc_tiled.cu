@@ -36,6 +36,7 @@
 namespace rg {
 
 static constexpr int kTP = 64;        // paths per tile
+static constexpr int kTiledMaxN = 768; // assets (K padded to 32, columns to 256)
 static constexpr int kTN = 128;       // assets per column block
 static constexpr int kTK = 8;         // K slice staged per step (warp-specialised form)
 static constexpr int kTiledThreads = 256;
@@ -531,11 +532,13 @@ __global__ void __launch_bounds__(kPipeThreads, 1) mc_tiled_pipe_kernel(const Ti
     float *partP = (float *)(partS + 16 * kTP);        // [16][kTP]
     __shared__ unsigned long long sacc[4];
     __shared__ unsigned int shist[VAR ? kVarHistBins + 2 : 1];
+    __shared__ float s_hmu[kTiledMaxN];                // H mu_c rounded to FP32, once per CTA
 
     const int tid = threadIdx.x;
     if (tid < 4) sacc[tid] = 0ull;
     if (VAR && a.var_mode == 2)
         for (int i = tid; i < a.sel_bins + 2; i += blockDim.x) shist[i] = 0u;
+    for (int c = tid; c < a.n; c += blockDim.x) s_hmu[c] = (float)((double)a.horizon * a.mu64[c]);
     __syncthreads();
     int crash = 0, breach = 0, n_tail = 0;
     long long tail_fx = 0;
@@ -671,7 +674,7 @@ __global__ void __launch_bounds__(kPipeThreads, 1) mc_tiled_pipe_kernel(const Ti
 #pragma unroll
                 for (int jj = 0; jj < 8; jj++) {
                     const int c = c0 + 8 * ag + jj;
-                    hm[jj] = (c < n) ? (float)((double)a.horizon * a.mu64[c]) : 0.f;
+                    hm[jj] = (c < n) ? s_hmu[c] : 0.f;
                     wt[jj] = (c < n) ? a.w[c] : 0.f;
                 }
 #pragma unroll
@@ -718,7 +721,7 @@ __global__ void __launch_bounds__(kPipeThreads, 1) mc_tiled_pipe_kernel(const Ti
     cta_flush(a, crash, breach, n_tail, tail_fx, sacc, VAR ? shist : nullptr, VAR);
 }
 
-int tiled_max_n() { return 768; }
+int tiled_max_n() { return kTiledMaxN; }
 
 size_t tiled_smem_bytes(int n, int kt, int threads)
 {
@@ -762,7 +765,8 @@ cudaError_t launch_tiled(const PlainArgs &a, const float *Lt, bool aggregated, i
         if (e == cudaSuccess) e = cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
         if (e != cudaSuccess) return e;
         const bool var = a.var_mode != 0;
-        const size_t static_bytes = 1024 + (var ? 4 * (size_t)(kVarHistBins + 2) : 0);
+        const size_t static_bytes =
+            1024 + 4 * (size_t)kTiledMaxN + (var ? 4 * (size_t)(kVarHistBins + 2) : 0); // + s_hmu
         // the widest L^T slice (32, 16 or 8 rows) whose shared memory fits
         const int kt = tiled_smem_bytes(a.n, 32, kTiledThreads) + static_bytes <= (size_t)optin   ? 32
                        : tiled_smem_bytes(a.n, 16, kTiledThreads) + static_bytes <= (size_t)optin ? 16
