@@ -68,6 +68,36 @@ def test_tc_per_path_parity(gpu, oracle, monkeypatch, kernel, prec, n, horizon, 
     assert r["breach_count"] == int((W < thr).sum())
 
 
+@pytest.mark.parametrize("M,offset", [(1, 0), (5, 3), (95, 0), (97, 1), (193, 1_000_003)])
+def test_tc_ragged_path_counts(gpu, oracle, M, offset):
+    """Tiles the paths fill only in part (1 path, one short of or one past a
+    96-path tile, an offset far from 0): every written path equals the oracle
+    and no slot past M is touched."""
+    import torch
+    n, horizon = 130, 2
+    code, near_tol, port_tol = CASES["bf16x3"]
+    mu, sigma, w = _case(n, 7)
+    x, k, thr, seed = 0.02 * math.sqrt(horizon), 13, -0.03, 91
+    port = gpu.Portfolio(mu, sigma, w)
+    S = torch.full((M + 8,), -1, dtype=torch.int32, device="cuda")
+    W = torch.full((M + 8,), float("nan"), dtype=torch.float32, device="cuda")
+    q = gpu.make_query(M, seed, x=x, k=k, horizon=horizon, port_threshold=thr, precision=code,
+                       d_s_values=S.data_ptr(), d_port_values=W.data_ptr(), path_offset=offset)
+    r = port.simulate(q)
+    torch.cuda.synchronize()
+    S, W = S.cpu().numpy(), W.cpu().numpy().astype(np.float64)
+    assert (S[M:] == -1).all() and np.isnan(W[M:]).all()
+    S, W = S[:M], W[:M]
+    L_ref, _ = oracle.cholesky_lower(sigma)
+    ref = oracle.mc_philox(mu, L_ref, w, horizon, M, seed, x, k, thr, want_S=True, want_port=True, want_R=True,
+                           path_offset=offset)
+    assert np.max(np.abs(W - ref["port"])) <= port_tol
+    near = np.min(np.abs(ref["R"] + x), axis=1) < near_tol
+    assert not ((S != ref["S"]) & ~near).any()
+    assert r["crash_count"] == int((S >= k).sum()) and r["breach_count"] == int((W < thr).sum())
+    port.close()
+
+
 @pytest.mark.parametrize("kernel", KERNELS)
 def test_tc_path_ranges_add_up(gpu, monkeypatch, kernel):
     """Counter-based draws: counts over [0, M) equal the sum over a split at
