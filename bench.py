@@ -83,6 +83,11 @@ NCU_TRAFFIC_BYTES = {"one_factor_50": 42_496, "five_factor_600": 1_000_000}
 # sampled SM clock it gives the kernel's issue bound: every SM issuing 4 warp
 # instructions (128 thread instructions) a cycle.
 TC_THREAD_INST_PER_NORMAL = 18.9
+# The same for the fused N = 50 kernel (mc_rows_kernel<13, true, false>):
+# thread instructions a path (ncu, 6.73e8 warp instructions for 1e7 paths;
+# 52 normals at about 15.8 instructions each plus 663 FFMA2, their L loads
+# and the per-row work).
+ROWS_THREAD_INST_PER_PATH = 2155
 
 
 def parse():
@@ -591,7 +596,7 @@ def batch_measure(steps, warmup, precision):
             "results_equal_alone_first16": same, "batch": info}
 
 
-def one_factor_50_measure(steps, warmup, flush, peaks):
+def one_factor_50_measure(steps, warmup, flush, peaks, sm_mhz=None):
     """The drop-in workload on the plain fused FP32 kernel: device paths/s,
     its roofline, and end to end through get_cuda_model().run_model."""
     import torch
@@ -611,6 +616,9 @@ def one_factor_50_measure(steps, warmup, flush, peaks):
     normals = 4 * ((n + 3) // 4)
     achieved = flops * M / (ms * 1e-3) / 1e12
     t_ideal = (flops / (peaks["fp32_tflops"] * 1e12) + normals / peaks["normals_per_s"]) * M
+    sms = torch.cuda.get_device_properties(torch.cuda.current_device()).multi_processor_count
+    mhz = sm_mhz or 2070.0
+    issue_bound = sms * 128 * mhz * 1e6 / ROWS_THREAD_INST_PER_PATH
     r = port.simulate(riskgpu.make_query(M, p.seed, x=p.x, k=p.k, horizon=1, port_threshold=p.port_threshold,
                                          precision=riskgpu.PREC_FP32, var_level=ALPHA))
     port.close()
@@ -631,6 +639,9 @@ def one_factor_50_measure(steps, warmup, flush, peaks):
             "roofline": {"bound": "alu", "achieved": achieved, "peak": peaks["fp32_tflops"], "unit": "TFLOP/s",
                          "frac": achieved / peaks["fp32_tflops"],
                          "composite_frac": t_ideal / (ms * 1e-3),
+                         "issue_bound": {"paths_per_s": issue_bound, "frac": M / (ms * 1e-3) / issue_bound,
+                                         "basis": f"{ROWS_THREAD_INST_PER_PATH} thread instructions per path (ncu) "
+                                                  f"at 128 a cycle on each of {sms} SMs, {mhz:.0f} MHz"},
                          "traffic": NCU_TRAFFIC_BYTES["one_factor_50"]},
             "counts": {"crash": crash, "breach": breach},
             "se_units": se_units(r, fig, M) if fig else why,
@@ -750,6 +761,14 @@ def engine_arm(args):
                     "normals_per_s": normals_per_s, "normals_peak": peaks["normals_per_s"],
                     "algorithmic_flops_per_path": flops_per_path,
                     "traffic": NCU_TRAFFIC_BYTES.get(key)}
+        if n == 50 and p.horizon == 1:
+            sms = torch.cuda.get_device_properties(torch.cuda.current_device()).multi_processor_count
+            mhz = clk.get("sm_mhz") or 2070.0
+            bound = sms * 128 * mhz * 1e6 / ROWS_THREAD_INST_PER_PATH
+            roofline["issue_bound"] = {
+                "paths_per_s": bound, "frac": count / (ms_per_step * 1e-3) / bound,
+                "basis": f"{ROWS_THREAD_INST_PER_PATH} thread instructions per path (ncu) at 128 a cycle on "
+                         f"each of {sms} SMs, {mhz:.0f} MHz"}
     if "fp32" in forms:
         f = forms["fp32"]
         t_ideal = (flops_per_path / (peaks["fp32_tflops"] * 1e12)
@@ -842,7 +861,8 @@ def engine_arm(args):
         torch.cuda.empty_cache()
         if not args.no_extras and args.workload == "five_factor_600":
             flush2 = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda")
-            line["one_factor_50"] = one_factor_50_measure(min(args.steps, 20), args.warmup, flush2, peaks)
+            line["one_factor_50"] = one_factor_50_measure(min(args.steps, 20), args.warmup, flush2, peaks,
+                                                          (line.get("clocks") or {}).get("sm_mhz"))
             del flush2
             line["batched"] = batch_measure(min(args.steps, 10), args.warmup, riskgpu.PREC_BF16X3)
             line["served"] = served_measure(1.0, riskgpu.PREC_BF16X3)
