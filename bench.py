@@ -79,10 +79,10 @@ NCU_TRAFFIC_BYTES = {"one_factor_50": 42_496, "five_factor_600": 1_000_000}
 
 # Thread instructions the tcgen05 kernel issues per normal it draws, daily
 # draws at N = 600, H = 10 (ncu smsp__inst_executed.sum of a 1e6-path launch,
-# 3.540e9 warp instructions x 32 / 6e9 normals).  With the SM count and the
+# 3.527e9 warp instructions x 32 / 6e9 normals).  With the SM count and the
 # sampled SM clock it gives the kernel's issue bound: every SM issuing 4 warp
 # instructions (128 thread instructions) a cycle.
-TC_THREAD_INST_PER_NORMAL = 18.9
+TC_THREAD_INST_PER_NORMAL = 18.8
 # The same for the fused N = 50 kernel (mc_rows_kernel<13, true, false>):
 # thread instructions a path (ncu, 6.73e8 warp instructions for 1e7 paths;
 # 52 normals at about 15.8 instructions each plus 663 FFMA2, their L loads
